@@ -1,0 +1,709 @@
+// nb_api.cu -- the C ABI of libnbody_gb300.so: handle life cycle, uploads,
+// downloads, and the DirectSum-on-GPU operations of AstroNbodySim.jl
+// (src/directsumgpu/gravity.jl, src/directsumgpu/timestep.jl) re-expressed as
+// launches of this library's kernels on the handle's stream.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nb_internal.cuh"
+
+using nb::Clock;
+using nb::TimeCfg;
+
+struct nb_handle {
+    nb_params p{};
+    TimeCfg tc{};
+    int dev = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int64_t n = 0;
+    int64_t cap = 0;
+    void* arena = nullptr;
+    double *x = nullptr, *y = nullptr, *z = nullptr;
+    double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+    double *ax = nullptr, *ay = nullptr, *az = nullptr;
+    double *pot = nullptr, *m = nullptr;
+    int32_t* type = nullptr;
+    int64_t *ti_beg = nullptr, *ti_end = nullptr;
+    int32_t* active = nullptr;
+    float4* pack = nullptr;
+    nb::dvec4* origin = nullptr;
+    int32_t ntiles = 0;
+    double* diag_scratch = nullptr;
+    int64_t diag_blocks = 0;
+    double* diag_out = nullptr;
+    Clock* clk = nullptr;
+    void* probe = nullptr;
+    size_t probe_bytes = 0;
+    cudaGraphExec_t step_exec = nullptr;
+    int block = 128;
+    int ipt = 2;
+    std::string err;
+};
+
+namespace {
+
+constexpr int kTileJ = 256;
+
+int fail(nb_handle* h, int code, const char* fmt, ...) {
+    if (h) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        h->err = buf;
+    }
+    return code;
+}
+
+#define NB_CK(call)                                                                            \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? NB_ERR_OOM : NB_ERR_CUDA,       \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+TimeCfg make_timecfg(const nb_params& p) {
+    TimeCfg c{};
+    c.adaptive = p.adaptive;
+    c.criterion = p.criterion;
+    c.dt = p.dt;
+    c.eta = p.eta;
+    c.min_step = p.min_step;
+    c.max_step = p.max_step;
+    c.time_base = p.time_base;
+    c.time_interval = (p.time_end - p.time_begin) / (double)p.time_base;
+    c.time_begin = p.time_begin;
+    for (int k = 0; k < 6; ++k) c.soft[k] = p.softening[k];
+    return c;
+}
+
+int check_params(nb_handle* h, const nb_params* p) {
+    if (!(p->law == NB_LAW_SPLINE_G2 || p->law == NB_LAW_PLUMMER))
+        return fail(h, NB_ERR_INVALID_ARG, "law must be NB_LAW_SPLINE_G2 or NB_LAW_PLUMMER");
+    if (!(p->precision == NB_PREC_FP64 || p->precision == NB_PREC_MIXED))
+        return fail(h, NB_ERR_INVALID_ARG, "precision must be NB_PREC_FP64 or NB_PREC_MIXED");
+    if (!(p->criterion == NB_CRIT_REF || p->criterion == NB_CRIT_ETA_SQRT_EPS))
+        return fail(h, NB_ERR_INVALID_ARG, "unknown timestep criterion");
+    for (int k = 0; k < 6; ++k)
+        if (!(p->softening[k] > 0.0) || !std::isfinite(p->softening[k]))
+            return fail(h, NB_ERR_INVALID_ARG, "softening[%d] must be finite and > 0", k);
+    if (!p->adaptive && !(p->dt > 0.0))
+        return fail(h, NB_ERR_INVALID_ARG, "constant timestep needs dt > 0");
+    if (p->adaptive) {
+        if (p->time_base <= 0 || (p->time_base & (p->time_base - 1)) != 0)
+            return fail(h, NB_ERR_INVALID_ARG, "time_base must be a power of two");
+        if (!(p->time_end > p->time_begin))
+            return fail(h, NB_ERR_INVALID_ARG, "time_end must exceed time_begin");
+        if (!(p->eta > 0.0)) return fail(h, NB_ERR_INVALID_ARG, "eta must be > 0");
+    }
+    const int b = p->block, i = p->i_per_thread;
+    if (b != 0 && b != 128 && b != 256) return fail(h, NB_ERR_INVALID_ARG, "block must be 128 or 256");
+    if (i != 0 && i != 1 && i != 2 && i != 4)
+        return fail(h, NB_ERR_INVALID_ARG, "i_per_thread must be 1, 2 or 4");
+    if (p->tile_j != 0 && p->tile_j != kTileJ)
+        return fail(h, NB_ERR_INVALID_ARG, "tile_j must be %d", kTileJ);
+    return NB_OK;
+}
+
+void drop_graph(nb_handle* h) {
+    if (h->step_exec) {
+        cudaGraphExecDestroy(h->step_exec);
+        h->step_exec = nullptr;
+    }
+}
+
+int sync_and_check(nb_handle* h) {
+    NB_CK(cudaStreamSynchronize(h->stream));
+    uint32_t e = 0;
+    NB_CK(cudaMemcpy(&e, &h->clk->err, sizeof e, cudaMemcpyDeviceToHost));
+    if (e) {
+        NB_CK(cudaMemset(&h->clk->err, 0, sizeof e));
+        if (e & nb::DEVERR_TIMEOUT)
+            return fail(h, NB_ERR_TIMEOUT, "device wait timed out (error bits 0x%x)", e);
+        return fail(h, NB_ERR_NUMERIC,
+                    "numeric error (bits 0x%x: 1=non-finite acc, 2=dt<MinStep, 4=bad integer step)",
+                    e);
+    }
+    return NB_OK;
+}
+
+nb::Targets particle_targets(nb_handle* h, bool active_only, bool want_acc, bool want_pot) {
+    nb::Targets t{};
+    t.x = h->x;
+    t.y = h->y;
+    t.z = h->z;
+    t.type = h->type;
+    t.idx = active_only ? h->active : nullptr;
+    t.d_count = active_only ? &h->clk->n_active : nullptr;
+    t.n = h->n;
+    for (int k = 0; k < 6; ++k) t.soft[k] = h->p.softening[k];
+    t.h_const = h->p.softening[0];
+    t.ax = want_acc ? h->ax : nullptr;
+    t.ay = want_acc ? h->ay : nullptr;
+    t.az = want_acc ? h->az : nullptr;
+    t.pot = want_pot ? h->pot : nullptr;
+    t.self_mass = h->m;
+    return t;
+}
+
+// Enqueue one force evaluation on stream s (no synchronisation).
+cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s) {
+    const bool pot = tg.pot != nullptr;
+    if (h->p.precision == NB_PREC_FP64) {
+        nb::Sources64 src{h->x, h->y, h->z, h->m, h->n};
+        return nb::launch_force_fp64(h->p.law, pot, src, tg, h->p.G, &h->clk->err, s);
+    }
+    cudaError_t e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, kTileJ, h->pack, h->origin, s);
+    if (e != cudaSuccess) return e;
+    nb::Sources32 src{h->pack, h->origin, h->ntiles, kTileJ};
+    return nb::launch_force_mixed(h->p.law, pot, src, tg, h->p.G, &h->clk->err, h->block, h->ipt,
+                                  s);
+}
+
+// Enqueue step(sim, DirectSum, GPU): drift -> force(active) -> kick.
+cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
+    cudaError_t e;
+    const bool adaptive = h->p.adaptive != 0;
+    if (adaptive) {
+        e = nb::launch_min_endstep(h->ti_end, h->n, h->p.time_base, h->clk, s);
+        if (e != cudaSuccess) return e;
+        e = nb::launch_drift(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->n, h->tc, h->clk, 0, 0, 0.0,
+                             s);
+        if (e != cudaSuccess) return e;
+        e = nb::launch_active_list(h->ti_end, h->n, h->clk, h->active, s);
+        if (e != cudaSuccess) return e;
+    } else {
+        e = nb::launch_drift(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->n, h->tc, h->clk, 2, 0, 0.0,
+                             s);
+        if (e != cudaSuccess) return e;
+    }
+    e = enqueue_force(h, particle_targets(h, adaptive, true, false), s);
+    if (e != cudaSuccess) return e;
+    e = nb::launch_kick(h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->type, h->ti_beg, h->ti_end,
+                        h->n, h->tc, h->clk, s);
+    if (e != cudaSuccess) return e;
+    return nb::launch_clock_end_step(h->clk, h->p.adaptive, s);
+}
+
+int ensure_capacity(nb_handle* h, int64_t n) {
+    if (n <= h->cap && h->arena) return NB_OK;
+    drop_graph(h);
+    if (h->arena) {
+        cudaFree(h->arena);
+        h->arena = nullptr;
+        h->cap = 0;
+    }
+    const int64_t ntiles = (n + kTileJ - 1) / kTileJ;
+    const int64_t npad = ntiles * kTileJ;
+    const int64_t dblocks = nb::diag_scratch_doubles(n);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off = align_up(off + bytes, 256);
+        return o;
+    };
+    const size_t d = sizeof(double) * (size_t)n;
+    size_t o_x = take(d), o_y = take(d), o_z = take(d), o_vx = take(d), o_vy = take(d),
+           o_vz = take(d), o_ax = take(d), o_ay = take(d), o_az = take(d), o_pot = take(d),
+           o_m = take(d);
+    size_t o_type = take(sizeof(int32_t) * (size_t)n);
+    size_t o_tb = take(sizeof(int64_t) * (size_t)n), o_te = take(sizeof(int64_t) * (size_t)n);
+    size_t o_act = take(sizeof(int32_t) * (size_t)n);
+    size_t o_pack = take(sizeof(float4) * (size_t)npad);
+    size_t o_orig = take(sizeof(nb::dvec4) * (size_t)ntiles);
+    size_t o_ds = take(sizeof(double) * (size_t)dblocks);
+    size_t o_do = take(sizeof(double) * 8);
+    void* a = nullptr;
+    NB_CK(cudaMalloc(&a, off));
+    char* b = static_cast<char*>(a);
+    h->arena = a;
+    h->cap = n;
+    h->x = (double*)(b + o_x);
+    h->y = (double*)(b + o_y);
+    h->z = (double*)(b + o_z);
+    h->vx = (double*)(b + o_vx);
+    h->vy = (double*)(b + o_vy);
+    h->vz = (double*)(b + o_vz);
+    h->ax = (double*)(b + o_ax);
+    h->ay = (double*)(b + o_ay);
+    h->az = (double*)(b + o_az);
+    h->pot = (double*)(b + o_pot);
+    h->m = (double*)(b + o_m);
+    h->type = (int32_t*)(b + o_type);
+    h->ti_beg = (int64_t*)(b + o_tb);
+    h->ti_end = (int64_t*)(b + o_te);
+    h->active = (int32_t*)(b + o_act);
+    h->pack = (float4*)(b + o_pack);
+    h->origin = (nb::dvec4*)(b + o_orig);
+    h->diag_scratch = (double*)(b + o_ds);
+    h->diag_blocks = dblocks / 8;
+    h->diag_out = (double*)(b + o_do);
+    h->ntiles = (int32_t)ntiles;
+    return NB_OK;
+}
+
+int require_particles(nb_handle* h) {
+    if (h->n <= 0) return fail(h, NB_ERR_STATE, "no particles uploaded");
+    return NB_OK;
+}
+
+int use_device(nb_handle* h) {
+    NB_CK(cudaSetDevice(h->dev));
+    return NB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nb_version(void) { return "nbody_gb300 0.1.0 (sm_103a)"; }
+
+void nb_default_params(nb_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->G = 1.0;
+    for (int k = 0; k < 6; ++k) p->softening[k] = 1.0e-4;
+    p->law = NB_LAW_SPLINE_G2;
+    p->precision = NB_PREC_MIXED;
+    p->adaptive = 1;
+    p->criterion = NB_CRIT_REF;
+    p->dt = 0.0;
+    p->eta = 0.025;
+    p->min_step = 1.0e-8;
+    p->max_step = INFINITY;
+    p->time_base = (int64_t)1 << 30;
+    p->time_begin = 0.0;
+    p->time_end = 0.1;
+    p->device = 0;
+}
+
+int nb_create(const nb_params* p, nb_handle** out) {
+    if (!p || !out) return NB_ERR_INVALID_ARG;
+    *out = nullptr;
+    nb_handle* h = new (std::nothrow) nb_handle();
+    if (!h) return NB_ERR_OOM;
+    int rc = check_params(h, p);
+    if (rc) {
+        delete h;
+        return rc;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || p->device < 0 || p->device >= ndev) {
+        delete h;
+        return NB_ERR_CUDA;
+    }
+    h->p = *p;
+    h->tc = make_timecfg(*p);
+    h->dev = p->device;
+    h->block = p->block ? p->block : 128;
+    h->ipt = p->i_per_thread ? p->i_per_thread : 2;
+    if (cudaSetDevice(h->dev) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&h->clk, sizeof(Clock)) != cudaSuccess) {
+        if (h->own_stream) cudaStreamDestroy(h->own_stream);
+        delete h;
+        return NB_ERR_CUDA;
+    }
+    h->stream = h->own_stream;
+    Clock c{};
+    c.t_float = p->time_begin;
+    c.last_t_float = p->time_begin;
+    cudaMemcpy(h->clk, &c, sizeof c, cudaMemcpyHostToDevice);
+    *out = h;
+    return NB_OK;
+}
+
+int nb_destroy(nb_handle* h) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    cudaSetDevice(h->dev);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graph(h);
+    if (h->arena) cudaFree(h->arena);
+    if (h->probe) cudaFree(h->probe);
+    if (h->clk) cudaFree(h->clk);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return NB_OK;
+}
+
+int nb_set_stream(nb_handle* h, void* stream) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    h->stream = stream ? static_cast<cudaStream_t>(stream) : h->own_stream;
+    return NB_OK;
+}
+
+int nb_get_stream(nb_handle* h, void** stream) {
+    if (!h || !stream) return NB_ERR_INVALID_ARG;
+    *stream = h->stream;
+    return NB_OK;
+}
+
+int nb_upload(nb_handle* h, int64_t n, const double* x, const double* y, const double* z,
+              const double* vx, const double* vy, const double* vz, const double* m,
+              const int32_t* type) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    if (n < 0 || n > (int64_t)0x7fffffff) return fail(h, NB_ERR_INVALID_ARG, "bad particle count %lld", (long long)n);
+    if (n > 0 && (!x || !y || !z || !vx || !vy || !vz || !m))
+        return fail(h, NB_ERR_INVALID_ARG, "null particle array");
+    if (type)
+        for (int64_t i = 0; i < n; ++i)
+            if (type[i] < 1 || type[i] > 6)
+                return fail(h, NB_ERR_INVALID_ARG, "type[%lld]=%d outside 1..6", (long long)i, type[i]);
+    int rc = use_device(h);
+    if (rc) return rc;
+    if (n > 0) {
+        rc = ensure_capacity(h, n);
+        if (rc) return rc;
+    }
+    h->n = n;
+    drop_graph(h);
+    if (n == 0) return NB_OK;
+    const size_t d = sizeof(double) * (size_t)n;
+    cudaStream_t s = h->stream;
+    NB_CK(cudaMemcpyAsync(h->x, x, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(h->y, y, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(h->z, z, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(h->vx, vx, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(h->vy, vy, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(h->vz, vz, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(h->m, m, d, cudaMemcpyHostToDevice, s));
+    if (type) {
+        NB_CK(cudaMemcpyAsync(h->type, type, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s));
+    } else {
+        // Default particle type 1.
+        std::vector<int32_t> ones((size_t)n, 1);
+        NB_CK(cudaMemcpy(h->type, ones.data(), sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice));
+    }
+    NB_CK(cudaMemsetAsync(h->ax, 0, d, s));
+    NB_CK(cudaMemsetAsync(h->ay, 0, d, s));
+    NB_CK(cudaMemsetAsync(h->az, 0, d, s));
+    NB_CK(cudaMemsetAsync(h->pot, 0, d, s));
+    NB_CK(cudaMemsetAsync(h->ti_beg, 0, sizeof(int64_t) * (size_t)n, s));
+    NB_CK(cudaMemsetAsync(h->ti_end, 0, sizeof(int64_t) * (size_t)n, s));
+    Clock c{};
+    c.t_float = h->p.time_begin;
+    c.last_t_float = h->p.time_begin;
+    NB_CK(cudaMemcpyAsync(h->clk, &c, sizeof c, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaStreamSynchronize(s));
+    return NB_OK;
+}
+
+int nb_download(nb_handle* h, double* x, double* y, double* z, double* vx, double* vy, double* vz,
+                double* ax, double* ay, double* az, double* pot, int64_t* ti_begstep,
+                int64_t* ti_endstep) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    if (h->n == 0) return NB_OK;
+    const size_t d = sizeof(double) * (size_t)h->n;
+    cudaStream_t s = h->stream;
+    struct {
+        void* dst;
+        const void* src;
+        size_t bytes;
+    } cp[] = {{x, h->x, d},   {y, h->y, d},   {z, h->z, d},   {vx, h->vx, d},
+              {vy, h->vy, d}, {vz, h->vz, d}, {ax, h->ax, d}, {ay, h->ay, d},
+              {az, h->az, d}, {pot, h->pot, d},
+              {ti_begstep, h->ti_beg, sizeof(int64_t) * (size_t)h->n},
+              {ti_endstep, h->ti_end, sizeof(int64_t) * (size_t)h->n}};
+    for (auto& c : cp)
+        if (c.dst) NB_CK(cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, s));
+    NB_CK(cudaStreamSynchronize(s));
+    return NB_OK;
+}
+
+int nb_upload_acc(nb_handle* h, const double* ax, const double* ay, const double* az) {
+    if (!h || !ax || !ay || !az) return fail(h, NB_ERR_INVALID_ARG, "null acceleration array");
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    const size_t d = sizeof(double) * (size_t)h->n;
+    NB_CK(cudaMemcpyAsync(h->ax, ax, d, cudaMemcpyHostToDevice, h->stream));
+    NB_CK(cudaMemcpyAsync(h->ay, ay, d, cudaMemcpyHostToDevice, h->stream));
+    NB_CK(cudaMemcpyAsync(h->az, az, d, cudaMemcpyHostToDevice, h->stream));
+    NB_CK(cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}
+
+int nb_upload_bins(nb_handle* h, const int64_t* ti_begstep, const int64_t* ti_endstep) {
+    if (!h || !ti_begstep || !ti_endstep) return fail(h, NB_ERR_INVALID_ARG, "null bin array");
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    const size_t d = sizeof(int64_t) * (size_t)h->n;
+    NB_CK(cudaMemcpyAsync(h->ti_beg, ti_begstep, d, cudaMemcpyHostToDevice, h->stream));
+    NB_CK(cudaMemcpyAsync(h->ti_end, ti_endstep, d, cudaMemcpyHostToDevice, h->stream));
+    NB_CK(cudaStreamSynchronize(h->stream));
+    return NB_OK;
+}
+
+int nb_set_softening(nb_handle* h, const double soft[6]) {
+    if (!h || !soft) return NB_ERR_INVALID_ARG;
+    for (int k = 0; k < 6; ++k)
+        if (!(soft[k] > 0.0) || !std::isfinite(soft[k]))
+            return fail(h, NB_ERR_INVALID_ARG, "softening[%d] must be finite and > 0", k);
+    for (int k = 0; k < 6; ++k) h->p.softening[k] = soft[k];
+    h->tc = make_timecfg(h->p);
+    drop_graph(h);
+    return NB_OK;
+}
+
+int nb_compute_force(nb_handle* h, int flags) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    const bool adaptive = h->p.adaptive != 0;
+    if (adaptive) NB_CK(nb::launch_active_list(h->ti_end, h->n, h->clk, h->active, h->stream));
+    NB_CK(enqueue_force(h, particle_targets(h, adaptive, true, (flags & NB_FORCE_POT) != 0),
+                        h->stream));
+    return sync_and_check(h);
+}
+
+int nb_compute_potential(nb_handle* h) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    NB_CK(enqueue_force(h, particle_targets(h, false, false, true), h->stream));
+    return sync_and_check(h);
+}
+
+int nb_remove_self_potential(nb_handle* h) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    NB_CK(nb::launch_remove_self_potential(h->pot, h->m, h->type, h->n, h->tc, h->p.G, h->stream));
+    return sync_and_check(h);
+}
+
+int nb_force_at_points(nb_handle* h, int64_t n, const double* px, const double* py,
+                       const double* pz, double soft, double* ax, double* ay, double* az,
+                       double* pot) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    if (n < 0 || n > (int64_t)0x7fffffff || (n > 0 && (!px || !py || !pz)))
+        return fail(h, NB_ERR_INVALID_ARG, "bad probe arrays");
+    if (!(soft > 0.0) || !std::isfinite(soft))
+        return fail(h, NB_ERR_INVALID_ARG, "softening must be finite and > 0");
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    if (n == 0) return NB_OK;
+    const size_t d = sizeof(double) * (size_t)n;
+    const size_t need = 7 * align_up(d, 256);
+    if (need > h->probe_bytes) {
+        if (h->probe) cudaFree(h->probe);
+        h->probe = nullptr;
+        h->probe_bytes = 0;
+        NB_CK(cudaMalloc(&h->probe, need));
+        h->probe_bytes = need;
+    }
+    char* b = static_cast<char*>(h->probe);
+    const size_t st = align_up(d, 256);
+    double* dx = (double*)(b + 0 * st);
+    double* dy = (double*)(b + 1 * st);
+    double* dz = (double*)(b + 2 * st);
+    double* oax = (double*)(b + 3 * st);
+    double* oay = (double*)(b + 4 * st);
+    double* oaz = (double*)(b + 5 * st);
+    double* opot = (double*)(b + 6 * st);
+    cudaStream_t s = h->stream;
+    NB_CK(cudaMemcpyAsync(dx, px, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(dy, py, d, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaMemcpyAsync(dz, pz, d, cudaMemcpyHostToDevice, s));
+    nb::Targets t{};
+    t.x = dx;
+    t.y = dy;
+    t.z = dz;
+    t.type = nullptr;
+    t.idx = nullptr;
+    t.d_count = nullptr;
+    t.n = n;
+    for (int k = 0; k < 6; ++k) t.soft[k] = soft;
+    t.h_const = soft;
+    const bool want_acc = ax || ay || az;
+    t.ax = want_acc ? oax : nullptr;
+    t.ay = want_acc ? oay : nullptr;
+    t.az = want_acc ? oaz : nullptr;
+    t.pot = pot ? opot : nullptr;
+    t.self_mass = nullptr;
+    NB_CK(enqueue_force(h, t, s));
+    if (ax) NB_CK(cudaMemcpyAsync(ax, oax, d, cudaMemcpyDeviceToHost, s));
+    if (ay) NB_CK(cudaMemcpyAsync(ay, oay, d, cudaMemcpyDeviceToHost, s));
+    if (az) NB_CK(cudaMemcpyAsync(az, oaz, d, cudaMemcpyDeviceToHost, s));
+    if (pot) NB_CK(cudaMemcpyAsync(pot, opot, d, cudaMemcpyDeviceToHost, s));
+    return sync_and_check(h);
+}
+
+int nb_init_timesteps(nb_handle* h) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    NB_CK(nb::launch_init_timesteps(h->ax, h->ay, h->az, h->type, h->ti_beg, h->ti_end, h->n, h->tc,
+                                    h->clk, h->stream));
+    return sync_and_check(h);
+}
+
+int nb_half_kick(nb_handle* h, int forward) {
+    if (!h || (forward != 1 && forward != -1)) return fail(h, NB_ERR_INVALID_ARG, "forward must be +1 or -1");
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    NB_CK(nb::launch_half_kick(h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->ti_beg, h->ti_end, h->n,
+                               h->tc, forward, h->stream));
+    return sync_and_check(h);
+}
+
+int nb_kick(nb_handle* h) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    NB_CK(nb::launch_kick(h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->type, h->ti_beg, h->ti_end,
+                          h->n, h->tc, h->clk, h->stream));
+    return sync_and_check(h);
+}
+
+int nb_find_min_endstep(nb_handle* h, int64_t* min_endstep) {
+    if (!h || !min_endstep) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    NB_CK(nb::launch_min_endstep(h->ti_end, h->n, h->p.time_base, h->clk, h->stream));
+    NB_CK(cudaMemcpyAsync(min_endstep, &h->clk->min_endstep, sizeof(int64_t),
+                          cudaMemcpyDeviceToHost, h->stream));
+    return sync_and_check(h);
+}
+
+int nb_drift_to_int(nb_handle* h, int64_t t_int) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    NB_CK(nb::launch_drift(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->n, h->tc, h->clk, 1, t_int, 0.0,
+                           h->stream));
+    return sync_and_check(h);
+}
+
+int nb_drift_to_float(nb_handle* h, double t_float) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    NB_CK(nb::launch_drift(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->n, h->tc, h->clk, 3, 0,
+                           t_float, h->stream));
+    return sync_and_check(h);
+}
+
+int nb_step(nb_handle* h, int64_t nsteps) {
+    if (!h || nsteps < 0) return fail(h, NB_ERR_INVALID_ARG, "nsteps must be >= 0");
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    if (nsteps == 0) return NB_OK;
+    if (!h->step_exec) {
+        // Capture one step on the handle's own (non-default) stream; the graph
+        // is then launched on whatever stream the handle currently uses.
+        cudaGraph_t g = nullptr;
+        NB_CK(cudaStreamSynchronize(h->stream));
+        NB_CK(cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_step(h, h->own_stream);
+        cudaError_t e2 = cudaStreamEndCapture(h->own_stream, &g);
+        if (e != cudaSuccess || e2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return fail(h, NB_ERR_CUDA, "step capture failed: %s",
+                        cudaGetErrorString(e != cudaSuccess ? e : e2));
+        }
+        e = cudaGraphInstantiate(&h->step_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            h->step_exec = nullptr;
+            return fail(h, NB_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+        }
+    }
+    for (int64_t k = 0; k < nsteps; ++k) NB_CK(cudaGraphLaunch(h->step_exec, h->stream));
+    return sync_and_check(h);
+}
+
+int nb_run_begin(nb_handle* h) {
+    int rc = nb_compute_force(h, 0);
+    if (rc) return rc;
+    rc = nb_init_timesteps(h);
+    if (rc) return rc;
+    return nb_half_kick(h, +1);
+}
+
+int nb_get_time(nb_handle* h, int64_t* t_int, double* t_float) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    Clock c{};
+    NB_CK(cudaStreamSynchronize(h->stream));
+    NB_CK(cudaMemcpy(&c, h->clk, sizeof c, cudaMemcpyDeviceToHost));
+    if (t_int) *t_int = c.t_int;
+    if (t_float) *t_float = c.t_float;
+    return NB_OK;
+}
+
+int nb_diagnostics(nb_handle* h, int with_potential, nb_diag* out) {
+    if (!h || !out) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    if (with_potential) NB_CK(enqueue_force(h, particle_targets(h, false, false, true), h->stream));
+    NB_CK(nb::launch_diag(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->m, h->pot, h->n,
+                          h->diag_scratch, h->diag_blocks, h->diag_out, h->stream));
+    double o[8];
+    NB_CK(cudaMemcpyAsync(o, h->diag_out, sizeof o, cudaMemcpyDeviceToHost, h->stream));
+    rc = sync_and_check(h);
+    if (rc) return rc;
+    out->kinetic = o[0];
+    out->potential = o[1];
+    for (int k = 0; k < 3; ++k) {
+        out->momentum[k] = o[2 + k];
+        out->angular_momentum[k] = o[5 + k];
+    }
+    return NB_OK;
+}
+
+int nb_active_count(nb_handle* h, int64_t* count) {
+    if (!h || !count) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    if (h->n == 0) {
+        *count = 0;
+        return NB_OK;
+    }
+    NB_CK(nb::launch_active_list(h->ti_end, h->n, h->clk, h->active, h->stream));
+    int32_t c = 0;
+    NB_CK(cudaMemcpyAsync(&c, &h->clk->n_active, sizeof c, cudaMemcpyDeviceToHost, h->stream));
+    NB_CK(cudaStreamSynchronize(h->stream));
+    *count = c;
+    return NB_OK;
+}
+
+const char* nb_last_error(nb_handle* h) {
+    if (!h) return "null handle";
+    return h->err.c_str();
+}
+
+}  // extern "C"

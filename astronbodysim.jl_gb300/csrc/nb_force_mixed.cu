@@ -1,0 +1,318 @@
+// nb_force_mixed.cu -- mixed-precision direct-sum force for sm_103a.
+//
+// Replaces compute_force_gpu_kernel (src/directsumgpu/gravity.jl:22-34), which
+// reads every source from global memory once per target thread, with:
+//   * a pack kernel that writes sources as FP32 float4 (x-o, y-o, z-o, m) in
+//     j-tiles of kTileJ particles, with an FP64 origin o per tile (the centre of
+//     the tile's bounding box);
+//   * a force kernel whose CTA holds BLOCK*IPT targets in registers and streams
+//     every j-tile through shared memory with bulk async copies
+//     (cp.async.bulk ... mbarrier::complete_tx, per CTA, no multicast) in an
+//     NSTAGE-deep ring.  Each target's position is re-expressed relative to the
+//     tile origin in FP64 once per tile, then the pair loop runs in FP32:
+//     3 FADD + FMUL + 2 FFMA (r^2), MUFU rsqrt, 3 FMUL, 3 FFMA per interaction.
+//     Per-tile FP32 partial sums are folded into (sum, carry) pairs with TwoSum.
+//
+// Pair law (per target softening h, src/directsum/gravity.jl:8-28):
+//   r >= h : a += m d / r^3                 (fast path, branch-free)
+//   r <  h : Gadget-2 spline polynomial     (rare slow path; includes j == i)
+// Potential (src/directsum/potential.jl:2-27): -m/r, spline inside h, 0 at r=0.
+#include <cstdio>
+
+#include "nb_internal.cuh"
+
+namespace nb {
+
+constexpr int kTileJ = 256;
+constexpr int kStages = 3;
+constexpr uint64_t kWaitTimeoutNs = 2000000000ull;  // 2 s
+
+// ---------------------------------------------------------------------------
+// Pack: one CTA of kTileJ threads per j-tile.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
+                                                 const double* __restrict__ y,
+                                                 const double* __restrict__ z,
+                                                 const double* __restrict__ m, int64_t n,
+                                                 float4* __restrict__ pack,
+                                                 dvec4* __restrict__ origin) {
+    __shared__ double red[6][kTileJ / 32];
+    const int64_t i = (int64_t)blockIdx.x * kTileJ + threadIdx.x;
+    const bool valid = i < n;
+    double px = 0.0, py = 0.0, pz = 0.0, pm = 0.0;
+    if (valid) {
+        px = x[i];
+        py = y[i];
+        pz = z[i];
+        pm = m[i];
+    }
+    double v[6];
+    v[0] = valid ? px : 1e300;
+    v[1] = valid ? py : 1e300;
+    v[2] = valid ? pz : 1e300;
+    v[3] = valid ? -px : 1e300;
+    v[4] = valid ? -py : 1e300;
+    v[5] = valid ? -pz : 1e300;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
+    }
+    __syncthreads();
+    double lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double a = red[k][0], b = red[k + 3][0];
+#pragma unroll
+        for (int w = 1; w < kTileJ / 32; ++w) {
+            a = fmin(a, red[k][w]);
+            b = fmin(b, red[k + 3][w]);
+        }
+        lo[k] = a;
+        hi[k] = -b;
+    }
+    // A tile with no valid particle cannot occur (tiles cover [0, n)).
+    const double ox = 0.5 * (lo[0] + hi[0]);
+    const double oy = 0.5 * (lo[1] + hi[1]);
+    const double oz = 0.5 * (lo[2] + hi[2]);
+    float4 q;
+    if (valid) {
+        q = make_float4((float)(px - ox), (float)(py - oy), (float)(pz - oz), (float)pm);
+    } else {
+        // Zero-mass padding far away: contributes exactly 0 and never takes the
+        // r < h path.
+        q = make_float4(1e18f, 1e18f, 1e18f, 0.0f);
+    }
+    pack[i] = q;
+    if (threadIdx.x == 0) origin[blockIdx.x] = make_dvec4(ox, oy, oz, 0.0);
+}
+
+cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
+                        int64_t n, int tile_j, float4* pack, dvec4* origin, cudaStream_t s) {
+    if (tile_j != kTileJ) return cudaErrorInvalidValue;
+    if (n <= 0) return cudaSuccess;
+    const int64_t ntiles = (n + kTileJ - 1) / kTileJ;
+    k_pack<<<(unsigned)ntiles, kTileJ, 0, s>>>(x, y, z, m, n, pack, origin);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Spline slow path (r < h), FP32.  Returns m*fac (to multiply d) in mr3 and the
+// negated potential contribution in mp.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void spline_close(float r2, float rinv, float m, float h, float& mr3,
+                                             float& mp) {
+    const float hinv = 1.0f / h;
+    const float hinv3 = hinv * hinv * hinv;
+    const float r = (r2 > 0.0f) ? r2 * rinv : 0.0f;
+    const float u = r * hinv;
+    float fac, wp;
+    if (u < 0.5f) {
+        fac = 10.666666666667f + u * u * (32.0f * u - 38.4f);
+        wp = -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f));
+    } else {
+        const float u3 = u * u * u;
+        fac = 21.333333333333f - 48.0f * u + 38.4f * u * u - 10.666666666667f * u3 -
+              0.066666666667f / u3;
+        wp = -3.2f + 0.066666666667f / u +
+             u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
+    }
+    mr3 = m * hinv3 * fac;
+    mp = (r2 > 0.0f) ? -(m * hinv * wp) : 0.0f;
+}
+
+// ---------------------------------------------------------------------------
+// Force kernel.
+// ---------------------------------------------------------------------------
+template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg, double G,
+                                                       uint32_t* __restrict__ err) {
+    __shared__ __align__(128) float4 buf[kStages * kTileJ];
+    __shared__ __align__(8) uint64_t full[kStages];
+
+    const int64_t ntg = tg.d_count ? (int64_t)(*tg.d_count) : tg.n;
+    const int64_t base = (int64_t)blockIdx.x * (BLOCK * IPT);
+    if (base >= ntg) return;  // CTA-uniform
+    const int tid = threadIdx.x;
+    const int ntiles = src.ntiles;
+
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        for (int s = 0; s < kStages && s < ntiles; ++s) {
+            mbar_arrive_expect_tx(&full[s], kTileJ * sizeof(float4));
+            bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)s * kTileJ, kTileJ * sizeof(float4),
+                     &full[s]);
+        }
+    }
+
+    int32_t pidx[IPT];
+    double px[IPT], py[IPT], pz[IPT];
+    float hh[IPT], h2[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int64_t t = base + k * BLOCK + tid;
+        pidx[k] = -1;
+        px[k] = 0.0;
+        py[k] = 0.0;
+        pz[k] = 0.0;
+        double h = tg.h_const;
+        if (t < ntg) {
+            const int32_t p = tg.idx ? tg.idx[t] : (int32_t)t;
+            pidx[k] = p;
+            px[k] = tg.x[p];
+            py[k] = tg.y[p];
+            pz[k] = tg.z[p];
+            if (tg.type) h = tg.soft[tg.type[p] - 1];
+        }
+        hh[k] = (float)h;
+        h2[k] = hh[k] * hh[k];
+    }
+
+    float sx[IPT], sy[IPT], sz[IPT], sp[IPT];
+    float cx[IPT], cy[IPT], cz[IPT], cp[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        sx[k] = sy[k] = sz[k] = sp[k] = 0.0f;
+        cx[k] = cy[k] = cz[k] = cp[k] = 0.0f;
+    }
+
+    for (int t = 0; t < ntiles; ++t) {
+        const int s = t % kStages;
+        const uint32_t par = (uint32_t)(t / kStages) & 1u;
+        const dvec4 o = src.origin[t];
+        float xr[IPT], yr[IPT], zr[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            xr[k] = (float)(px[k] - o.x);
+            yr[k] = (float)(py[k] - o.y);
+            zr[k] = (float)(pz[k] - o.z);
+        }
+        float ax[IPT], ay[IPT], az[IPT], ap[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = ap[k] = 0.0f;
+
+        const bool ok = mbar_wait_bounded(&full[s], par, kWaitTimeoutNs);
+        if (ok) {
+            const float4* b = &buf[s * kTileJ];
+#pragma unroll 4
+            for (int j = 0; j < kTileJ; ++j) {
+                const float4 q = b[j];
+#pragma unroll
+                for (int k = 0; k < IPT; ++k) {
+                    const float dx = q.x - xr[k];
+                    const float dy = q.y - yr[k];
+                    const float dz = q.z - zr[k];
+                    float r2;
+                    if (LAW == NB_LAW_PLUMMER)
+                        r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, h2[k])));
+                    else
+                        r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    const float rinv = rsqrt_approx(r2);
+                    float mp = q.w * rinv;
+                    float mr3 = mp * rinv * rinv;
+                    if (LAW == NB_LAW_SPLINE_G2) {
+                        if (__builtin_expect(r2 < h2[k], 0)) spline_close(r2, rinv, q.w, hh[k], mr3, mp);
+                    }
+                    if (ACC) {
+                        ax[k] = fmaf(dx, mr3, ax[k]);
+                        ay[k] = fmaf(dy, mr3, ay[k]);
+                        az[k] = fmaf(dz, mr3, az[k]);
+                    }
+                    if (POT) ap[k] -= mp;
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            if (ACC) {
+                two_sum_acc(sx[k], cx[k], ax[k]);
+                two_sum_acc(sy[k], cy[k], ay[k]);
+                two_sum_acc(sz[k], cz[k], az[k]);
+            }
+            if (POT) two_sum_acc(sp[k], cp[k], ap[k]);
+        }
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(err, DEVERR_TIMEOUT);
+                // Drain the copies this CTA still has in flight before exiting.
+                for (int u = t; u < t + kStages && u < ntiles; ++u)
+                    (void)mbar_wait_bounded(&full[u % kStages], (uint32_t)(u / kStages) & 1u,
+                                            kWaitTimeoutNs);
+            }
+            return;
+        }
+        if (tid == 0 && t + kStages < ntiles) {
+            mbar_arrive_expect_tx(&full[s], kTileJ * sizeof(float4));
+            bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)(t + kStages) * kTileJ,
+                     kTileJ * sizeof(float4), &full[s]);
+        }
+    }
+
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int32_t p = pidx[k];
+        if (p < 0) continue;
+        if (ACC) {
+            tg.ax[p] = ((double)sx[k] + (double)cx[k]) * G;
+            tg.ay[p] = ((double)sy[k] + (double)cy[k]) * G;
+            tg.az[p] = ((double)sz[k] + (double)cz[k]) * G;
+        }
+        if (POT) {
+            double phi = (double)sp[k] + (double)cp[k];
+            if (LAW == NB_LAW_PLUMMER && tg.self_mass) {
+                // Remove the self pair, bit-identical to the term the loop added.
+                const float mself = (float)tg.self_mass[p];
+                phi += (double)(mself * rsqrt_approx(h2[k]));
+            }
+            tg.pot[p] = phi * G;
+        }
+    }
+}
+
+template <int LAW, bool ACC, bool POT>
+static cudaError_t launch_cfg(const Sources32& src, const Targets& tg, double G, uint32_t* err,
+                              int block, int ipt, cudaStream_t s) {
+    const int64_t per = (int64_t)block * ipt;
+    const int64_t grid = (tg.n + per - 1) / per;
+    if (grid <= 0) return cudaSuccess;
+#define NB_LAUNCH(B, I)                                                           \
+    if (block == B && ipt == I) {                                                 \
+        k_force_mixed<LAW, ACC, POT, B, I><<<(unsigned)grid, B, 0, s>>>(src, tg, G, err); \
+        return cudaGetLastError();                                                \
+    }
+    NB_LAUNCH(128, 1)
+    NB_LAUNCH(128, 2)
+    NB_LAUNCH(128, 4)
+    NB_LAUNCH(256, 1)
+    NB_LAUNCH(256, 2)
+    NB_LAUNCH(256, 4)
+#undef NB_LAUNCH
+    return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_force_mixed(int law, bool pot, const Sources32& src, const Targets& tg,
+                               double G, uint32_t* err, int block, int ipt, cudaStream_t s) {
+    if (src.tile_j != kTileJ) return cudaErrorInvalidValue;
+    const bool acc = tg.ax != nullptr;
+    if (!acc && !pot) return cudaSuccess;
+    if (law == NB_LAW_PLUMMER) {
+        if (!acc) return launch_cfg<NB_LAW_PLUMMER, false, true>(src, tg, G, err, block, ipt, s);
+        return pot ? launch_cfg<NB_LAW_PLUMMER, true, true>(src, tg, G, err, block, ipt, s)
+                   : launch_cfg<NB_LAW_PLUMMER, true, false>(src, tg, G, err, block, ipt, s);
+    }
+    if (!acc) return launch_cfg<NB_LAW_SPLINE_G2, false, true>(src, tg, G, err, block, ipt, s);
+    return pot ? launch_cfg<NB_LAW_SPLINE_G2, true, true>(src, tg, G, err, block, ipt, s)
+               : launch_cfg<NB_LAW_SPLINE_G2, true, false>(src, tg, G, err, block, ipt, s);
+}
+
+}  // namespace nb

@@ -1,0 +1,220 @@
+// nb_internal.cuh -- device-side layout, kernel argument blocks and PTX helpers
+// shared by the translation units of libnbody_gb300.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nbody_gb300.h"
+
+namespace nb {
+
+// 32-byte aligned FP64 quadruple (tile origins, staged FP64 sources).
+struct __align__(32) dvec4 {
+    double x, y, z, w;
+};
+__host__ __device__ __forceinline__ dvec4 make_dvec4(double x, double y, double z, double w) {
+    return dvec4{x, y, z, w};
+}
+
+// Device error word bits (read back by the host after synchronising calls).
+enum : uint32_t {
+    DEVERR_NONFINITE = 1u,  // NaN/Inf acceleration
+    DEVERR_MINSTEP = 2u,    // dt < MinStep   (src/base/Timestep.jl:9-11)
+    DEVERR_TISTEP = 4u,     // ti_step <= 0   (src/base/Timestep.jl:13-16)
+    DEVERR_TIMEOUT = 8u,    // bounded mbarrier wait gave up
+};
+
+// Device-resident time line (TimeInfo) and per-step scalars.
+struct Clock {
+    int64_t t_int;          // system_time_int
+    int64_t last_t_int;     // last_system_time_int
+    int64_t min_endstep;    // find_min_endstep result
+    double t_float;         // system_time_float
+    double last_t_float;    // last_system_time_float
+    double dt_drift;        // interval of the pending drift
+    int32_t n_active;       // active particles at t_int
+    uint32_t err;           // DEVERR_* bits
+};
+
+// Timestep configuration passed by value.
+struct TimeCfg {
+    int32_t adaptive;
+    int32_t criterion;
+    double dt;
+    double eta;
+    double min_step;
+    double max_step;
+    int64_t time_base;
+    double time_interval;
+    double time_begin;
+    double soft[6];
+};
+
+// Targets of a force evaluation.  Target slot t maps to particle idx[t]
+// (identity when idx == nullptr); positions and outputs are indexed by the
+// particle index.  The number of targets is *d_count when d_count != nullptr,
+// else n.
+struct Targets {
+    const double* x;
+    const double* y;
+    const double* z;
+    const int32_t* type;  // softening table index 1..6; nullptr -> h_const
+    const int32_t* idx;
+    const int32_t* d_count;
+    int64_t n;
+    double soft[6];
+    double h_const;
+    double* ax;
+    double* ay;
+    double* az;
+    double* pot;  // nullptr -> no potential
+    // Plummer law only: targets are also sources at the same FP32 position
+    // (the self pair contributes -m/h to the potential and is removed).
+    const double* self_mass;
+};
+
+// Packed FP32 sources for the mixed kernel: j-tiles of tile_j particles,
+// float4 (x - o, y - o, z - o, m) with an FP64 origin o per tile.
+struct Sources32 {
+    const float4* pack;
+    const dvec4* origin;
+    int32_t ntiles;
+    int32_t tile_j;
+};
+
+// FP64 sources.
+struct Sources64 {
+    const double* x;
+    const double* y;
+    const double* z;
+    const double* m;
+    int64_t n;
+};
+
+// Launch helpers implemented in the .cu files.
+cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
+                        int64_t n, int tile_j, float4* pack, dvec4* origin, cudaStream_t s);
+cudaError_t launch_force_mixed(int law, bool pot, const Sources32& src, const Targets& tg,
+                               double G, uint32_t* err, int block, int ipt, cudaStream_t s);
+cudaError_t launch_force_fp64(int law, bool pot, const Sources64& src, const Targets& tg,
+                              double G, uint32_t* err, cudaStream_t s);
+
+// Integrator kernels (nb_integrate.cu).
+cudaError_t launch_active_list(const int64_t* ti_end, int64_t n, Clock* clk, int32_t* list,
+                               cudaStream_t s);
+cudaError_t launch_init_timesteps(const double* ax, const double* ay, const double* az,
+                                  const int32_t* type, int64_t* ti_beg, int64_t* ti_end, int64_t n,
+                                  TimeCfg cfg, Clock* clk, cudaStream_t s);
+cudaError_t launch_half_kick(double* vx, double* vy, double* vz, const double* ax,
+                             const double* ay, const double* az, const int64_t* ti_beg,
+                             const int64_t* ti_end, int64_t n, TimeCfg cfg, int forward,
+                             cudaStream_t s);
+cudaError_t launch_kick(double* vx, double* vy, double* vz, const double* ax, const double* ay,
+                        const double* az, const int32_t* type, int64_t* ti_beg, int64_t* ti_end,
+                        int64_t n, TimeCfg cfg, Clock* clk, cudaStream_t s);
+cudaError_t launch_min_endstep(const int64_t* ti_end, int64_t n, int64_t time_base, Clock* clk,
+                               cudaStream_t s);
+// mode 0: drift to clk->min_endstep (adaptive); 1: to t_int_arg; 2: float t + dt (const step);
+// 3: to t_float_arg.
+cudaError_t launch_drift(double* x, double* y, double* z, const double* vx, const double* vy,
+                         const double* vz, int64_t n, TimeCfg cfg, Clock* clk, int mode,
+                         int64_t t_int_arg, double t_float_arg, cudaStream_t s);
+cudaError_t launch_clock_end_step(Clock* clk, int adaptive, cudaStream_t s);
+cudaError_t launch_diag(const double* x, const double* y, const double* z, const double* vx,
+                        const double* vy, const double* vz, const double* m, const double* pot,
+                        int64_t n, double* scratch, int64_t scratch_blocks, double* out8,
+                        cudaStream_t s);
+int64_t diag_scratch_doubles(int64_t n);
+cudaError_t launch_remove_self_potential(double* pot, const double* m, const int32_t* type,
+                                         int64_t n, TimeCfg cfg, double G, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// PTX helpers (sm_90+ mbarrier / bulk async copy).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: gives up after ~timeout_ns of wall time (globaltimer) or an
+// iteration cap, whichever comes first.  Returns false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  uint64_t timeout_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0; it < (1u << 26); ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255u) == 255u && globaltimer_ns() - t0 > timeout_ns) return false;
+    }
+    return false;
+}
+
+// Bulk global->shared copy completing on an mbarrier (no multicast).
+// dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Knuth TwoSum accumulation: (s, c) += v with the rounding error of s + v
+// carried in c.
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float v) {
+    float t = s + v;
+    float bp = t - s;
+    float e = (s - (t - bp)) + (v - bp);
+    s = t;
+    c += e;
+}
+
+__device__ __forceinline__ void two_sum_acc(double& s, double& c, double v) {
+    double t = __dadd_rn(s, v);
+    double bp = __dadd_rn(t, -s);
+    double e = __dadd_rn(__dadd_rn(s, -__dadd_rn(t, -bp)), __dadd_rn(v, -bp));
+    s = t;
+    c = __dadd_rn(c, e);
+}
+
+}  // namespace nb

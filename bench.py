@@ -1,0 +1,369 @@
+"""Benchmark of the direct-sum hot path on one GB300 (replicas per GPU for N > 1).
+
+Workload: Plummer sphere N = 2^20 (G = M = a = 1), equal masses, softening
+eps = 1e-3 (Gadget-2 spline law, the reference's pair law), mixed precision
+(FP32 pairs relative to FP64 tile origins, compensated sums, FP64 state),
+constant-step leapfrog at dt = 1e-4.  One step = one KDK step of
+step(sim, DirectSum, GPU): drift, FP32 pack, force on all N targets from all N
+sources (N^2 interactions), kick -- one CUDA-graph replay.
+
+Prints one JSON line (rank 0).  `value` = interactions/s of the timed steps with
+state resident in HBM; `e2e` = the same metric through the public API with the
+state copied from pinned host memory before and back after every step.
+`--impl reference` times the CPU Float64 restatement of the reference's direct
+sum (the oracle) on all host cores instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG_ROOT = os.path.join(REPO, "astronbodysim.jl_gb300")
+for _p in (REPO, PKG_ROOT):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "G interactions/s at N=2^20, mixed vs FP64 at stated error; batch p50/p99 latency"
+UNIT = "G interactions/s"
+N_DEFAULT = 1 << 20
+EPS = 1.0e-3
+DT = 1.0e-4
+FLOP_PER_INTERACTION = 20
+L2_FLUSH_BYTES = 256 << 20
+STEP_KERNELS = 6  # clock advance, drift, pack, force, kick, clock end
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_rate(data, n_targets, seed=7, nthreads=0):
+    """Oracle (CPU Float64 restatement of src/directsum/gravity.jl:37-46, 80-101)
+    on a bounded sample: n_targets seeded targets x all sources."""
+    from oracle import oracle
+
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(data["pos"].shape[0], size=n_targets, replace=False)
+    t0 = time.perf_counter()
+    oracle.force(data["pos"], data["mass"], data["pos"][idx], EPS, want_pot=False,
+                 nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return n_targets * data["pos"].shape[0] / dt, dt, oracle.max_threads() if nthreads == 0 else nthreads
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import astronbodysim as nb
+
+    n = args.n
+    data = nb.plummer(n, seed=2)
+    targets = args.ref_targets
+    for _ in range(args.warmup):
+        cpu_oracle_rate(data, targets)
+    total_pairs, total_t, cores = 0.0, 0.0, 1
+    for k in range(args.steps):
+        rate, dt, cores = cpu_oracle_rate(data, targets, seed=100 + k)
+        total_pairs += rate * dt
+        total_t += dt
+    v = total_pairs / total_t / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Plummer sphere)",
+        "config": {"workload": "plummer_n%d_eps1e-3_spline" % n, "n": n,
+                   "sample": "%d seeded targets x %d sources per step" % (targets, n)},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d targets x %d sources per step, OpenMP static blocks" % (targets, n)},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import torch
+
+    import astronbodysim as nb
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = args.n
+    data = nb.plummer(n, seed=2 + rank)
+    sim = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
+                        precision="mixed", law=args.law, device=local, block=args.block,
+                        i_per_thread=args.ipt)
+    stream = torch.cuda.Stream(device=dev)
+    sim.set_stream(stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    # ---- force accuracy vs the oracle on a seeded subsample (rank 0) -------
+    acc_stats = {}
+    if rank == 0 and not args.skip_accuracy:
+        from oracle import oracle
+
+        rng = np.random.default_rng(1234)
+        sub = np.sort(rng.choice(n, size=args.acc_targets, replace=False))
+        nb.compute_force(sim, want_potential=True)
+        g = nb.get_all_data(sim)
+        a_ref, p_ref = oracle.force(data["pos"], data["mass"], data["pos"][sub], EPS,
+                                    law=oracle.LAW_SPLINE_G2 if args.law == "spline" else oracle.LAW_PLUMMER)
+        e = np.linalg.norm(g["acc"][sub] - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+        ep = np.abs(g["pot"][sub] - p_ref) / np.abs(p_ref)
+        acc_stats["mixed"] = {"force_rel_median": float(np.median(e)),
+                              "force_rel_p99": float(np.quantile(e, 0.99)),
+                              "force_rel_max": float(e.max()),
+                              "pot_rel_median": float(np.median(ep)),
+                              "pot_rel_p99": float(np.quantile(ep, 0.99))}
+        # plain FP64 form on the same targets (probe points at the particles)
+        sim64 = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
+                              precision="fp64", law=args.law, device=local)
+        nb.force_and_potential_at_points(sim64, data["pos"][sub[:256]], EPS)  # warm-up
+        t0 = time.perf_counter()
+        a64, p64 = nb.force_and_potential_at_points(sim64, data["pos"][sub], EPS)
+        t64 = time.perf_counter() - t0
+        e64 = np.linalg.norm(a64 - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+        ep64 = np.abs(p64 - p_ref) / np.abs(p_ref)
+        acc_stats["fp64"] = {"force_rel_max": float(e64.max()), "pot_rel_max": float(ep64.max()),
+                             "g_interactions_per_s_force_and_potential": len(sub) * n / t64 / 1e9,
+                             "sample": "%d targets x %d sources, force+potential, host timer" % (len(sub), n)}
+        sim64.close()
+        acc_stats["targets"] = int(len(sub))
+
+    # ---- resident run: warm-up, then K timed steps ------------------------
+    nb.run  # noqa: B018  (API reference for readers)
+    sim._ck(sim._lib.nb_run_begin(sim.handle))
+    for _ in range(args.warmup):
+        nb.step(sim, 1)
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    ev = []
+    torch.cuda.synchronize(dev)
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)  # L2 flush (256 MiB write), outside the events
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        nb.step(sim, 1)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        ev.append((e0, e1))
+    torch.cuda.synchronize(dev)
+    t_wall = time.perf_counter() - t_wall0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+
+    # ---- force kernel alone (roofline), same stream ------------------------
+    fev = []
+    for _ in range(args.force_reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        nb.compute_force(sim)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        fev.append((e0, e1))
+    torch.cuda.synchronize(dev)
+    clocks = sampler.stop()
+    force_ms = statistics.mean(a.elapsed_time(b) for a, b in fev)
+
+    # ---- end to end through the public API with host buffers ---------------
+    pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+           for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "m")}
+    ptype = torch.ones(n, dtype=torch.int32, pin_memory=True).numpy()
+    st = nb.get_all_data(sim)
+    for k, col in (("x", st["pos"][:, 0]), ("y", st["pos"][:, 1]), ("z", st["pos"][:, 2]),
+                   ("vx", st["vel"][:, 0]), ("vy", st["vel"][:, 1]), ("vz", st["vel"][:, 2]),
+                   ("ax", st["acc"][:, 0]), ("ay", st["acc"][:, 1]), ("az", st["acc"][:, 2])):
+        pin[k][:] = col
+    pin["m"][:] = data["mass"]
+    from astronbodysim import _lib as L
+
+    lib = sim._lib
+    h2d = 7 * 8 * n + 4 * n + 3 * 8 * n
+    d2h = 9 * 8 * n
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        sim._ck(lib.nb_upload(sim.handle, n, *[L.dptr(pin[k]) for k in ("x", "y", "z", "vx", "vy", "vz", "m")],
+                              L.i32ptr(ptype)))
+        sim._ck(lib.nb_upload_acc(sim.handle, L.dptr(pin["ax"]), L.dptr(pin["ay"]), L.dptr(pin["az"])))
+        nb.step(sim, 1)
+        sim._ck(lib.nb_download(sim.handle, *[L.dptr(pin[k]) for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az")],
+                                None, None, None))
+    t_e2e = time.perf_counter() - t0
+
+    # ---- aggregate over ranks (replicas) -----------------------------------
+    total_s = total_ms / 1e3
+    if ws > 1:
+        t = torch.tensor([total_s, t_e2e], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s, t_e2e = float(t[0]), float(t[1])
+    pairs = float(n) * float(n)
+    value = ws * args.steps * pairs / total_s / 1e9
+    e2e_value = ws * args.e2e_steps * pairs / t_e2e / 1e9
+
+    if rank == 0:
+        peaks = measured_peaks()
+        props = torch.cuda.get_device_properties(dev)
+        sm_max = peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0
+        fp32_peak_tflops = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+        achieved = FLOP_PER_INTERACTION * pairs / (force_ms / 1e3) / 1e12
+        traffic = None
+        tpath = os.path.join(REPO, "profiles", "force_mixed_traffic.json")
+        if os.path.exists(tpath):
+            try:
+                with open(tpath) as f:
+                    tj = json.load(f)
+                traffic = tj.get("bytes_per_launch_scaled_to_n%d" % n)
+            except Exception:
+                traffic = None
+        cpu = None
+        if not args.skip_cpu_baseline:
+            rate, dt, cores = cpu_oracle_rate(data, args.cpu_targets)
+            cpu = {"value": rate / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": "%d seeded targets x %d sources (%.1f s), OpenMP static blocks, FP64"
+                             % (args.cpu_targets, n, dt)}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Plummer sphere, G=M=a=1)",
+            "config": {"workload": "plummer_n%d_eps1e-3_%s_mixed_kdk_dt1e-4" % (n, args.law),
+                       "n": n, "law": args.law, "precision": "mixed (fp32 pairs, fp64 origins/state)",
+                       "step": "drift+pack+force(N^2)+kick, one CUDA graph replay",
+                       "l2": "256 MiB write between timed steps, outside the events",
+                       "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "block": sim.params.block or 128, "i_per_thread": sim.params.i_per_thread or 2},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak_tflops,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak_tflops, "traffic": traffic,
+                         "kernel": "k_force_mixed (+k_pack)", "force_ms": force_ms,
+                         "peak_note": "FP32 peak = SMs x 128 lanes x 2 x sm_max_mhz (%s); 20 flop/interaction"
+                                      % ("MEASURED_PEAKS.json" if peaks.get("sm_max_mhz") else "nvidia-smi")},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
+            "gpu_launches": STEP_KERNELS * args.steps,
+            "clocks": clocks,
+            "accuracy": acc_stats,
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--law", default="spline", choices=["spline", "plummer"])
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--ipt", type=int, default=0)
+    ap.add_argument("--force-reps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--acc-targets", type=int, default=4096)
+    ap.add_argument("--cpu-targets", type=int, default=2048)
+    ap.add_argument("--ref-targets", type=int, default=1024)
+    ap.add_argument("--skip-accuracy", action="store_true")
+    ap.add_argument("--skip-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,187 @@
+/*
+ * nbody_gb300.h -- C ABI of libnbody_gb300.so, the GB300 (sm_103a) direct-sum
+ * gravity engine that stands in for AstroNbodySim.jl's DirectSum GPU device.
+ *
+ * Every entry point is plain C (pointers, sizes, status codes).  The library
+ * owns all device memory behind an opaque handle; host arrays are read only
+ * during an upload call and written only during a download call.  One CUDA
+ * stream per handle; calls on one handle must be serialised by the caller,
+ * distinct handles may be driven from different threads.
+ *
+ * Reference interfaces each entry point replaces are cited as
+ * path:line inside the AstroNbodySim.jl project.
+ */
+#ifndef NBODY_GB300_H
+#define NBODY_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (0 = success) -------------------------------------- */
+#define NB_OK 0
+#define NB_ERR_INVALID_ARG -1
+#define NB_ERR_OOM -2
+#define NB_ERR_CUDA -3
+#define NB_ERR_NUMERIC -4  /* NaN/Inf acceleration, dt < MinStep, bad integer step
+                              (src/base/Timestep.jl:9-16) */
+#define NB_ERR_TIMEOUT -5  /* a bounded device-side wait gave up */
+#define NB_ERR_ADMISSION -6 /* batch/serve: request does not fit the footprint budget */
+#define NB_ERR_STATE -7    /* call out of order (e.g. no particles uploaded) */
+#define NB_ERR_NOT_FOUND -8 /* batch/serve: unknown request id */
+
+/* ---- enums ----------------------------------------------------------- */
+#define NB_LAW_SPLINE_G2 0 /* Gadget-2 cubic spline, src/directsum/gravity.jl:8-28 */
+#define NB_LAW_PLUMMER 1   /* a = G m d / (r^2 + h^2)^(3/2) */
+
+#define NB_PREC_FP64 0  /* plain FP64 pair arithmetic, the reference's Float64 form */
+#define NB_PREC_MIXED 1 /* FP32 pairs relative to FP64 tile origins, compensated sums */
+
+#define NB_CRIT_REF 0          /* dt = sqrt(2 eta h / |a|), src/base/Timestep.jl:3 */
+#define NB_CRIT_ETA_SQRT_EPS 1 /* dt = eta sqrt(h / |a|) */
+
+/* flags of nb_compute_force */
+#define NB_FORCE_POT 1 /* also write the potential per unit mass */
+
+typedef struct nb_handle nb_handle;
+
+/* Mirrors the SimConfig keywords relevant to DirectSum on GPU
+ * (src/base/Config.jl:515-628, TimeConfig :408-449, GravityConfig :106-169). */
+typedef struct nb_params {
+    double G;             /* sim.config.constants.G (units stripped by the caller) */
+    double softening[6];  /* ForceSofteningTable, indexed by particle type 1..6 */
+    int32_t law;          /* NB_LAW_* */
+    int32_t precision;    /* NB_PREC_* */
+    int32_t adaptive;     /* 0: ConstantTimestep(dt); 1: AdaptiveTimestep */
+    int32_t criterion;    /* NB_CRIT_* (adaptive only) */
+    double dt;            /* TimeStep (constant) */
+    double eta;           /* ErrTolTimestep (default 0.025) */
+    double min_step;      /* MinStep (default 1e-8) */
+    double max_step;      /* MaxStep (default +Inf) */
+    int64_t time_base;    /* TimeBase (default 1<<30) */
+    double time_begin;    /* TimeBegin */
+    double time_end;      /* TimeEnd; TimeInterval = (end-begin)/time_base */
+    int32_t device;       /* CUDA ordinal */
+    int32_t tile_j;       /* tuning override: j-tile (0 = auto) */
+    int32_t i_per_thread; /* tuning override (0 = auto) */
+    int32_t block;        /* tuning override: threads per CTA (0 = auto) */
+} nb_params;
+
+/* Energy / momentum diagnostics, FP64 (src/base/Energy.jl:13-101). */
+typedef struct nb_diag {
+    double kinetic;   /* sum 0.5 m v.v */
+    double potential; /* 0.5 sum m phi (src/directsum/potential.jl:150-153) */
+    double momentum[3];
+    double angular_momentum[3];
+} nb_diag;
+
+/* Fill *p with the reference defaults (G=1, softening 1e-4, spline, mixed,
+ * adaptive, eta 0.025, MinStep 1e-8, MaxStep Inf, TimeBase 2^30, [0, 0.1]). */
+void nb_default_params(nb_params *p);
+
+/* Create a handle on p->device.  Replaces the GPU branch of the Simulation
+ * constructor's data placement (src/base/Config.jl:1072-1088). */
+int nb_create(const nb_params *p, nb_handle **out);
+int nb_destroy(nb_handle *h);
+
+/* Use the caller's CUDA stream (a cudaStream_t passed as void*) instead of the
+ * handle's own; NULL restores the handle's own stream. */
+int nb_set_stream(nb_handle *h, void *stream);
+int nb_get_stream(nb_handle *h, void **stream);
+
+/* Upload n particles, SoA FP64; type[i] in 1..6 (Collection index into the
+ * softening table, src/base/Config.jl:108).  Resets the time line (t_int = 0,
+ * t_float = time_begin), Ti_begstep = Ti_endstep = 0, Acc = 0.
+ * Replaces cu(StructArray(d)) at src/base/Config.jl:1072-1088. */
+int nb_upload(nb_handle *h, int64_t n, const double *x, const double *y, const double *z,
+              const double *vx, const double *vy, const double *vz, const double *m,
+              const int32_t *type);
+
+/* Download state; any pointer may be NULL.  Replaces get_all_data / get_local_data
+ * (src/base/Config.jl:1199-1201, 1228-1230). */
+int nb_download(nb_handle *h, double *x, double *y, double *z, double *vx, double *vy,
+                double *vz, double *ax, double *ay, double *az, double *pot,
+                int64_t *ti_begstep, int64_t *ti_endstep);
+
+/* Overwrite accelerations / integer time bins (restart, tests). */
+int nb_upload_acc(nb_handle *h, const double *ax, const double *ay, const double *az);
+int nb_upload_bins(nb_handle *h, const int64_t *ti_begstep, const int64_t *ti_endstep);
+
+/* Replaces set_softlen! for GPU (src/tools/SofteningLength.jl:87-89).
+ * Every entry must be > 0 (h = 0 makes the reference's self pair 0/0). */
+int nb_set_softening(nb_handle *h, const double soft[6]);
+
+/* Acceleration of the active particles (Ti_endstep == system_time_int), all of
+ * them in constant-step mode; inactive particles keep their Acc as on the CPU
+ * path.  flags & NB_FORCE_POT also writes the potential of the same particles.
+ * Replaces compute_force(sim, DirectSum, GPU) (src/directsumgpu/gravity.jl:36-45,
+ * 81-85) with CPU semantics (src/directsum/gravity.jl:92-101). */
+int nb_compute_force(nb_handle *h, int flags);
+
+/* Potential per unit mass of every particle.  New GPU method for
+ * compute_potential(sim, DirectSum, CPU) (src/directsum/potential.jl:142-148). */
+int nb_compute_potential(nb_handle *h);
+
+/* Self-potential term of src/base/Potential.jl:5-24: pot += G m / (h / 2.8)
+ * for every particle (h from its type), as compute_potential(sim) applies it
+ * after the direct sum (src/base/Potential.jl:21-24). */
+int nb_remove_self_potential(nb_handle *h);
+
+/* Acceleration and potential at n probe points (host arrays) with softening
+ * length soft, from all resident particles.  Replaces
+ * compute_force(sim, pos, SoftLength) (src/directsum/gravity.jl:180-193) and
+ * compute_potential(sim, pos, SoftLength) (src/directsum/potential.jl:171-181).
+ * Any output pointer may be NULL. */
+int nb_force_at_points(nb_handle *h, int64_t n, const double *px, const double *py,
+                       const double *pz, double soft, double *ax, double *ay, double *az,
+                       double *pot);
+
+/* init_timesteps (src/base/Timestep.jl:29-44; GPU src/directsumgpu/timestep.jl:32-47). */
+int nb_init_timesteps(nb_handle *h);
+
+/* leapfrog_half_kick with forward = +1 / -1 (src/base/Timestep.jl:105-133;
+ * GPU src/directsumgpu/timestep.jl:178-214). */
+int nb_half_kick(nb_handle *h, int forward);
+
+/* advance_and_find_timestep (src/base/Timestep.jl:47-101; GPU :122-174). */
+int nb_kick(nb_handle *h);
+
+/* find_min_endstep (src/base/Timestep.jl:135-144; GPU src/directsumgpu/timestep.jl:103-114). */
+int nb_find_min_endstep(nb_handle *h, int64_t *min_endstep);
+
+/* drift_particles_adaptive_timestep to an integer time (src/directsum/timestep.jl:1-20)
+ * and drift_particles_const_timestep to a float time (:22-38). */
+int nb_drift_to_int(nb_handle *h, int64_t t_int);
+int nb_drift_to_float(nb_handle *h, double t_float);
+
+/* nsteps of step(sim, DirectSum, GPU) (src/directsumgpu/timestep.jl:216-224):
+ * drift to the next sync point, force on active particles, kick.  The step is
+ * captured once in a CUDA graph and replayed; the time line lives on the device. */
+int nb_step(nb_handle *h, int64_t nsteps);
+
+/* src/run.jl:76-87: force, init_timesteps, forward half kick. */
+int nb_run_begin(nb_handle *h);
+
+/* System time (TimeInfo.system_time_int / system_time_float). */
+int nb_get_time(nb_handle *h, int64_t *t_int, double *t_float);
+
+/* FP64 diagnostics; with_potential != 0 first recomputes the potential
+ * (src/base/Energy.jl:13-101, src/directsum/potential.jl:150-153). */
+int nb_diagnostics(nb_handle *h, int with_potential, nb_diag *out);
+
+/* Number of particles active at the current time (Ti_endstep == t_int). */
+int nb_active_count(nb_handle *h, int64_t *count);
+
+/* Last error message of this handle (never NULL). */
+const char *nb_last_error(nb_handle *h);
+
+/* Library version string. */
+const char *nb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBODY_GB300_H */

@@ -1,0 +1,207 @@
+"""GPU parity: libnbody_gb300.so through its C ABI against the oracle and the
+golden known answers.  Tolerances:
+  FP64 form   : |a_gpu - a_oracle| <= 1e-12 |a_oracle| per force (and potential)
+  mixed form  : median relative force error <= 1e-6, p99 <= 1e-5
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def make_sim(nb, data, **kw):
+    return nb.Simulation(data, **kw)
+
+
+def rel_err(a, b):
+    return np.linalg.norm(a - b, axis=-1) / np.linalg.norm(b, axis=-1)
+
+
+@pytest.fixture(scope="module")
+def plummer4096(nb):
+    return nb.plummer(4096, seed=1)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_binary_static(nb, golden, precision):
+    """test/StaticTest.jl:161-207 through the GPU path."""
+    g = golden("binary_static.json")
+    data = {"pos": np.array(g["pos"]), "vel": np.array(g["vel"]), "mass": np.full(2, g["mass"])}
+    sim = make_sim(nb, data, G=g["G"], ForceSofteningTable=[g["softening"]] * 6,
+                   ErrTolTimestep=g["eta"], precision=precision)
+    nb.compute_force(sim)
+    d = nb.get_all_data(sim)
+    a = d["acc"]
+    rtol = g["rtol"] if precision == "fp64" else 1e-6
+    assert abs(a[0, 0] + a[1, 0]) <= rtol * abs(a[0, 0])
+    np.testing.assert_allclose(abs(a[:, 0]), g["acc_abs"], rtol=rtol)
+    np.testing.assert_allclose(nb.total_potential(sim), g["potential"], rtol=rtol)
+    np.testing.assert_allclose(nb.total_kinetic(sim), g["kinetic"], rtol=g["rtol"])
+    np.testing.assert_allclose(nb.total_energy(sim), g["energy"], rtol=rtol)
+    nb.init_timesteps(sim)
+    d = nb.get_all_data(sim)
+    dt_sim = (d["ti_endstep"][0] - d["ti_begstep"][0]) * sim.TimeInterval
+    assert dt_sim < g["dt_bound"]
+    P = nb.total_momentum(sim)
+    assert np.all(np.abs(P) <= g["rtol"] * g["mass"] * abs(g["vel"][0][1]))
+    np.testing.assert_allclose(nb.total_angular_momentum(sim), g["angular_momentum"],
+                               rtol=g["rtol"], atol=1e-30)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_box_probe(nb, golden, precision):
+    """test/StaticTest.jl:299-350: force and potential at a probe point."""
+    g = golden("box_probe.json")
+    pos = np.array(g["pos"])
+    data = {"pos": pos, "vel": np.zeros_like(pos), "mass": np.full(len(pos), g["mass"])}
+    sim = make_sim(nb, data, G=g["G"], ForceSofteningTable=[g["softening"]] * 6, precision=precision)
+    acc, pot = nb.force_and_potential_at_points(sim, np.array([g["probe"]]), g["softening"])
+    rtol = 1e-14 if precision == "fp64" else 2e-6
+    np.testing.assert_allclose(acc[0], g["acc"], rtol=rtol)
+    np.testing.assert_allclose(pot[0], g["pot"], rtol=rtol)
+
+
+@pytest.mark.parametrize("law", ["spline", "plummer"])
+def test_fp64_force_matches_oracle_1e12(nb, oracle, plummer4096, law):
+    """Plain FP64 GPU form vs the CPU Float64 direct sum: <= 1e-12 relative per force."""
+    d = plummer4096
+    h = 0.01
+    sim = make_sim(nb, d, ForceSofteningTable=[h] * 6, precision="fp64", law=law)
+    nb.compute_force(sim, want_potential=True)
+    g = nb.get_all_data(sim)
+    olaw = oracle.LAW_SPLINE_G2 if law == "spline" else oracle.LAW_PLUMMER
+    a_ref, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], h, law=olaw)
+    e = rel_err(g["acc"], a_ref)
+    assert e.max() <= 1e-12, e.max()
+    ep = np.abs(g["pot"] - p_ref) / np.abs(p_ref)
+    assert ep.max() <= 1e-12, ep.max()
+
+
+@pytest.mark.parametrize("law", ["spline", "plummer"])
+def test_mixed_force_error_quantiles(nb, oracle, plummer4096, law):
+    d = plummer4096
+    h = 0.01
+    sim = make_sim(nb, d, ForceSofteningTable=[h] * 6, precision="mixed", law=law)
+    nb.compute_force(sim, want_potential=True)
+    g = nb.get_all_data(sim)
+    olaw = oracle.LAW_SPLINE_G2 if law == "spline" else oracle.LAW_PLUMMER
+    a_ref, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], h, law=olaw)
+    e = rel_err(g["acc"], a_ref)
+    ep = np.abs(g["pot"] - p_ref) / np.abs(p_ref)
+    assert np.median(e) <= 1e-6, np.median(e)
+    assert np.quantile(e, 0.99) <= 1e-5, np.quantile(e, 0.99)
+    assert np.median(ep) <= 1e-6 and np.quantile(ep, 0.99) <= 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("n", [1, 2, 3, 255, 256, 257, 1000])
+def test_ragged_sizes(nb, oracle, precision, n):
+    """Ragged tiles, single particle (zero force), tiny systems."""
+    d = nb.plummer(n, seed=n) if n > 1 else {"pos": np.zeros((1, 3)) + 0.25, "vel": np.zeros((1, 3)),
+                                              "mass": np.ones(1)}
+    h = 0.05
+    sim = make_sim(nb, d, ForceSofteningTable=[h] * 6, precision=precision)
+    nb.compute_force(sim, want_potential=True)
+    g = nb.get_all_data(sim)
+    a_ref, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], h)
+    if n == 1:
+        assert np.all(g["acc"] == 0.0) and g["pot"][0] == 0.0
+        return
+    tol = 1e-12 if precision == "fp64" else 3e-5
+    e = rel_err(g["acc"], a_ref)
+    assert e.max() <= tol, e.max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_close_pairs_spline_branch(nb, oracle, precision):
+    """Particles inside each other's softening length exercise r < h, both
+    spline segments, and exactly coincident particles (r == 0)."""
+    rng = np.random.default_rng(7)
+    n = 600
+    pos = rng.normal(scale=0.02, size=(n, 3))
+    pos[10] = pos[11]  # coincident pair
+    d = {"pos": pos, "vel": np.zeros_like(pos), "mass": rng.uniform(0.5, 1.5, n) / n}
+    h = 0.02
+    sim = make_sim(nb, d, ForceSofteningTable=[h] * 6, precision=precision)
+    nb.compute_force(sim, want_potential=True)
+    g = nb.get_all_data(sim)
+    a_ref, p_ref = oracle.force(pos, d["mass"], pos, h)
+    e = rel_err(g["acc"], a_ref)
+    ep = np.abs(g["pot"] - p_ref) / np.abs(p_ref)
+    if precision == "fp64":
+        assert e.max() <= 1e-12 and ep.max() <= 1e-12
+    else:
+        assert np.median(e) <= 1e-5 and np.median(ep) <= 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_far_offset_system(nb, oracle, precision):
+    """A system far from the coordinate origin: the FP64 tile origins keep the
+    mixed form's relative coordinates small."""
+    d = nb.plummer(2048, seed=5)
+    pos = d["pos"] + np.array([1.0e5, -3.0e4, 2.0e4])
+    dd = {"pos": pos, "vel": d["vel"], "mass": d["mass"]}
+    h = 0.01
+    sim = make_sim(nb, dd, ForceSofteningTable=[h] * 6, precision=precision)
+    nb.compute_force(sim)
+    g = nb.get_all_data(sim)
+    a_ref, _ = oracle.force(pos, d["mass"], pos, h)
+    e = rel_err(g["acc"], a_ref)
+    if precision == "fp64":
+        assert e.max() <= 1e-10
+    else:
+        # positions ~1e5: FP32 relative coordinates within a tile keep ~1e-7 of the tile size
+        assert np.median(e) <= 1e-4
+
+
+def test_softening_table_by_type(nb, oracle):
+    """Per-type softening (ForceSofteningTable indexed by Collection)."""
+    d = nb.plummer(1024, seed=9)
+    types = (np.arange(1024) % 6 + 1).astype(np.int32)
+    table = [0.01, 0.02, 0.05, 0.1, 0.2, 0.3]
+    dd = dict(d, collection=types)
+    sim = make_sim(nb, dd, ForceSofteningTable=table, precision="fp64")
+    nb.compute_force(sim, want_potential=True)
+    g = nb.get_all_data(sim)
+    th = np.array(table)[types - 1]
+    a_ref, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], th)
+    assert rel_err(g["acc"], a_ref).max() <= 1e-12
+    assert (np.abs(g["pot"] - p_ref) / np.abs(p_ref)).max() <= 1e-12
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_probe_points_match_oracle(nb, oracle, plummer4096, precision):
+    d = plummer4096
+    rng = np.random.default_rng(11)
+    probes = rng.normal(size=(300, 3))
+    sim = make_sim(nb, d, ForceSofteningTable=[0.01] * 6, precision=precision)
+    acc, pot = nb.force_and_potential_at_points(sim, probes, 0.02)
+    a_ref, p_ref = oracle.force(d["pos"], d["mass"], probes, 0.02)
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    assert rel_err(acc, a_ref).max() <= tol
+    assert (np.abs(pot - p_ref) / np.abs(p_ref)).max() <= tol
+
+
+def test_compute_potential_self_term(nb, oracle):
+    """compute_potential(sim) adds +G m / (h / 2.8) as src/base/Potential.jl:5-24 does."""
+    d = nb.plummer(512, seed=2)
+    h = 0.01
+    sim = make_sim(nb, d, ForceSofteningTable=[h] * 6, precision="fp64", G=2.0)
+    nb.compute_potential(sim)
+    g = nb.get_all_data(sim)
+    _, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], h, G=2.0)
+    p_ref = p_ref + 2.0 * d["mass"] / (h / 2.8)
+    np.testing.assert_allclose(g["pot"], p_ref, rtol=1e-12)
+
+
+def test_invalid_arguments(nb):
+    d = nb.plummer(64, seed=1)
+    with pytest.raises(nb.NbodyError):
+        nb.Simulation(d, ForceSofteningTable=[0.0] * 6)
+    sim = nb.Simulation(d, ForceSofteningTable=[0.01] * 6)
+    with pytest.raises(nb.NbodyError):
+        nb.leapfrog_half_kick(sim, 2)
+    with pytest.raises(nb.NbodyError):
+        sim.upload(dict(d, collection=np.full(64, 9, dtype=np.int32)))
+    with pytest.raises(nb.NbodyError):
+        nb.set_softlen(sim, [0.01, 0.01, -1.0, 0.01, 0.01, 0.01])
