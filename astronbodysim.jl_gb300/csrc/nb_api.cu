@@ -30,6 +30,8 @@ struct nb_handle {
     int32_t* type = nullptr;
     int64_t *ti_beg = nullptr, *ti_end = nullptr;
     int32_t* active = nullptr;
+    int32_t* perm = nullptr;
+    void* sort_scratch = nullptr;
     float4* pack = nullptr;
     nb::dvec4* origin = nullptr;
     int32_t ntiles = 0;
@@ -162,10 +164,17 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s) {
         nb::Sources64 src{h->x, h->y, h->z, h->m, h->n};
         return nb::launch_force_fp64(h->p.law, pot, src, tg, h->p.G, &h->clk->err, s);
     }
-    cudaError_t e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, kTileJ, h->pack, h->origin, s);
+    // Morton order of the sources keeps every j-tile compact, so the FP32
+    // coordinates relative to its origin stay small.
+    cudaError_t e = nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, s);
+    if (e != cudaSuccess) return e;
+    e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, s);
     if (e != cudaSuccess) return e;
     nb::Sources32 src{h->pack, h->origin, h->ntiles, kTileJ};
-    return nb::launch_force_mixed(h->p.law, pot, src, tg, h->p.G, &h->clk->err, h->block, h->ipt,
+    nb::Targets t2 = tg;
+    // All-particle evaluations visit the targets in the same Morton order.
+    if (!t2.idx && t2.x == h->x) t2.idx = h->perm;
+    return nb::launch_force_mixed(h->p.law, pot, src, t2, h->p.G, &h->clk->err, h->block, h->ipt,
                                   s);
 }
 
@@ -218,6 +227,8 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     size_t o_type = take(sizeof(int32_t) * (size_t)n);
     size_t o_tb = take(sizeof(int64_t) * (size_t)n), o_te = take(sizeof(int64_t) * (size_t)n);
     size_t o_act = take(sizeof(int32_t) * (size_t)n);
+    size_t o_perm = take(sizeof(int32_t) * (size_t)n);
+    size_t o_sort = take(nb::sort_scratch_bytes(n));
     size_t o_pack = take(sizeof(float4) * (size_t)npad);
     size_t o_orig = take(sizeof(nb::dvec4) * (size_t)ntiles);
     size_t o_ds = take(sizeof(double) * (size_t)dblocks);
@@ -242,6 +253,8 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->ti_beg = (int64_t*)(b + o_tb);
     h->ti_end = (int64_t*)(b + o_te);
     h->active = (int32_t*)(b + o_act);
+    h->perm = (int32_t*)(b + o_perm);
+    h->sort_scratch = (void*)(b + o_sort);
     h->pack = (float4*)(b + o_pack);
     h->origin = (nb::dvec4*)(b + o_orig);
     h->diag_scratch = (double*)(b + o_ds);

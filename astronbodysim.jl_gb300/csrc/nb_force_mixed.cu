@@ -28,12 +28,15 @@ constexpr int kStages = 3;
 constexpr uint64_t kWaitTimeoutNs = 2000000000ull;  // 2 s
 
 // ---------------------------------------------------------------------------
-// Pack: one CTA of kTileJ threads per j-tile.
+// Pack: one CTA of kTileJ threads per j-tile.  Slot i of the packed array holds
+// particle perm[i] (identity when perm == nullptr); the tile origin is the
+// centre of the tile's FP64 bounding box and origin.w its half diagonal.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
                                                  const double* __restrict__ y,
                                                  const double* __restrict__ z,
                                                  const double* __restrict__ m, int64_t n,
+                                                 const int32_t* __restrict__ perm,
                                                  float4* __restrict__ pack,
                                                  dvec4* __restrict__ origin) {
     __shared__ double red[6][kTileJ / 32];
@@ -41,10 +44,11 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
     const bool valid = i < n;
     double px = 0.0, py = 0.0, pz = 0.0, pm = 0.0;
     if (valid) {
-        px = x[i];
-        py = y[i];
-        pz = z[i];
-        pm = m[i];
+        const int64_t p = perm ? (int64_t)perm[i] : i;
+        px = x[p];
+        py = y[p];
+        pz = z[p];
+        pm = m[p];
     }
     double v[6];
     v[0] = valid ? px : 1e300;
@@ -76,7 +80,7 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
         lo[k] = a;
         hi[k] = -b;
     }
-    // A tile with no valid particle cannot occur (tiles cover [0, n)).
+    // Every tile holds at least one particle (tiles cover [0, n)).
     const double ox = 0.5 * (lo[0] + hi[0]);
     const double oy = 0.5 * (lo[1] + hi[1]);
     const double oz = 0.5 * (lo[2] + hi[2]);
@@ -89,15 +93,19 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
         q = make_float4(1e18f, 1e18f, 1e18f, 0.0f);
     }
     pack[i] = q;
-    if (threadIdx.x == 0) origin[blockIdx.x] = make_dvec4(ox, oy, oz, 0.0);
+    if (threadIdx.x == 0) {
+        const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+        origin[blockIdx.x] = make_dvec4(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
+    }
 }
 
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
-                        int64_t n, int tile_j, float4* pack, dvec4* origin, cudaStream_t s) {
+                        int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
+                        cudaStream_t s) {
     if (tile_j != kTileJ) return cudaErrorInvalidValue;
     if (n <= 0) return cudaSuccess;
     const int64_t ntiles = (n + kTileJ - 1) / kTileJ;
-    k_pack<<<(unsigned)ntiles, kTileJ, 0, s>>>(x, y, z, m, n, pack, origin);
+    k_pack<<<(unsigned)ntiles, kTileJ, 0, s>>>(x, y, z, m, n, perm, pack, origin);
     return cudaGetLastError();
 }
 

@@ -94,7 +94,13 @@ struct Sources64 {
 
 // Launch helpers implemented in the .cu files.
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
-                        int64_t n, int tile_j, float4* pack, dvec4* origin, cudaStream_t s);
+                        int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
+                        cudaStream_t s);
+// Morton-order permutation of the particles (nb_sort.cu); scratch of
+// sort_scratch_bytes(n) bytes.
+size_t sort_scratch_bytes(int64_t n);
+cudaError_t launch_morton_sort(const double* x, const double* y, const double* z, int64_t n,
+                               void* scratch, int32_t* perm, cudaStream_t s);
 cudaError_t launch_force_mixed(int law, bool pot, const Sources32& src, const Targets& tg,
                                double G, uint32_t* err, int block, int ipt, cudaStream_t s);
 cudaError_t launch_force_fp64(int law, bool pot, const Sources64& src, const Targets& tg,

@@ -95,7 +95,9 @@ def test_circular_binary_const_leapfrog(nb, golden, precision):
                         TimeEnd=g["time_end"], precision=precision)
     nb.run(sim)
     p = nb.get_all_data(sim)["pos"]
-    rtol = g["rtol"] if precision == "fp64" else 1e-5
+    # mixed: FP32 pair forces (~1e-7 relative) accumulate into the orbital phase
+    # over 2899 steps (one full orbit)
+    rtol = g["rtol"] if precision == "fp64" else 1e-4
     np.testing.assert_allclose(p[0, 0], g["x_end"], rtol=rtol)
     np.testing.assert_allclose(p[0, 1], g["y_end"], rtol=rtol)
 

@@ -1,7 +1,8 @@
 """GPU parity: libnbody_gb300.so through its C ABI against the oracle and the
 golden known answers.  Tolerances:
   FP64 form   : |a_gpu - a_oracle| <= 1e-12 |a_oracle| per force (and potential)
-  mixed form  : median relative force error <= 1e-6, p99 <= 1e-5
+  mixed form  : median relative force error <= 1e-6, p99 <= 1e-5, max <= 1e-4
+                (sources in Morton order, FP32 pairs relative to FP64 tile origins)
 """
 import numpy as np
 import pytest
@@ -90,6 +91,7 @@ def test_mixed_force_error_quantiles(nb, oracle, plummer4096, law):
     ep = np.abs(g["pot"] - p_ref) / np.abs(p_ref)
     assert np.median(e) <= 1e-6, np.median(e)
     assert np.quantile(e, 0.99) <= 1e-5, np.quantile(e, 0.99)
+    assert e.max() <= 1e-4, e.max()
     assert np.median(ep) <= 1e-6 and np.quantile(ep, 0.99) <= 1e-5
 
 
@@ -107,9 +109,11 @@ def test_ragged_sizes(nb, oracle, precision, n):
     if n == 1:
         assert np.all(g["acc"] == 0.0) and g["pot"][0] == 0.0
         return
-    tol = 1e-12 if precision == "fp64" else 3e-5
     e = rel_err(g["acc"], a_ref)
-    assert e.max() <= tol, e.max()
+    if precision == "fp64":
+        assert e.max() <= 1e-12, e.max()
+    else:
+        assert np.median(e) <= 1e-6 and e.max() <= 1e-4, (np.median(e), e.max())
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -177,9 +181,12 @@ def test_probe_points_match_oracle(nb, oracle, plummer4096, precision):
     sim = make_sim(nb, d, ForceSofteningTable=[0.01] * 6, precision=precision)
     acc, pot = nb.force_and_potential_at_points(sim, probes, 0.02)
     a_ref, p_ref = oracle.force(d["pos"], d["mass"], probes, 0.02)
-    tol = 1e-12 if precision == "fp64" else 1e-5
-    assert rel_err(acc, a_ref).max() <= tol
-    assert (np.abs(pot - p_ref) / np.abs(p_ref)).max() <= tol
+    e = rel_err(acc, a_ref)
+    ep = np.abs(pot - p_ref) / np.abs(p_ref)
+    if precision == "fp64":
+        assert e.max() <= 1e-12 and ep.max() <= 1e-12
+    else:
+        assert np.median(e) <= 1e-6 and e.max() <= 1e-4 and ep.max() <= 1e-5
 
 
 def test_compute_potential_self_term(nb, oracle):
@@ -190,8 +197,10 @@ def test_compute_potential_self_term(nb, oracle):
     nb.compute_potential(sim)
     g = nb.get_all_data(sim)
     _, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], h, G=2.0)
-    p_ref = p_ref + 2.0 * d["mass"] / (h / 2.8)
-    np.testing.assert_allclose(g["pot"], p_ref, rtol=1e-12)
+    corr = 2.0 * d["mass"] / (h / 2.8)
+    # the +2.8 G m / h term nearly cancels phi for some particles: bound the
+    # error by the magnitude of the direct sum itself
+    np.testing.assert_allclose(g["pot"], p_ref + corr, rtol=0, atol=1e-12 * np.abs(p_ref).max())
 
 
 def test_invalid_arguments(nb):
