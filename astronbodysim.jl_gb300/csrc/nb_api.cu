@@ -138,14 +138,14 @@ int sync_and_check(nb_handle* h) {
     return NB_OK;
 }
 
-nb::Targets particle_targets(nb_handle* h, bool active_only, bool want_acc, bool want_pot) {
+nb::Targets particle_targets(nb_handle* h, bool want_acc, bool want_pot) {
     nb::Targets t{};
     t.x = h->x;
     t.y = h->y;
     t.z = h->z;
     t.type = h->type;
-    t.idx = active_only ? h->active : nullptr;
-    t.d_count = active_only ? &h->clk->n_active : nullptr;
+    t.idx = nullptr;
+    t.d_count = nullptr;
     t.n = h->n;
     for (int k = 0; k < 6; ++k) t.soft[k] = h->p.softening[k];
     t.h_const = h->p.softening[0];
@@ -157,23 +157,43 @@ nb::Targets particle_targets(nb_handle* h, bool active_only, bool want_acc, bool
     return t;
 }
 
-// Enqueue one force evaluation on stream s (no synchronisation).
-cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s) {
+// Enqueue one force evaluation on stream s (no synchronisation).  With
+// active_only the targets are the particles with Ti_endstep == t_int
+// (src/directsum/gravity.jl:95-96); the list is built on the device.
+cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, bool active_only) {
     const bool pot = tg.pot != nullptr;
+    const bool particles = tg.x == h->x;
+    nb::Targets t2 = tg;
+    cudaError_t e;
     if (h->p.precision == NB_PREC_FP64) {
+        if (active_only) {
+            e = nb::launch_active_list(h->ti_end, h->n, nullptr, h->clk, h->active, s);
+            if (e != cudaSuccess) return e;
+            t2.idx = h->active;
+            t2.d_count = &h->clk->n_active;
+        }
         nb::Sources64 src{h->x, h->y, h->z, h->m, h->n};
-        return nb::launch_force_fp64(h->p.law, pot, src, tg, h->p.G, &h->clk->err, s);
+        return nb::launch_force_fp64(h->p.law, pot, src, t2, h->p.G, &h->clk->err, s);
     }
     // Morton order of the sources keeps every j-tile compact, so the FP32
     // coordinates relative to its origin stay small.
-    cudaError_t e = nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, s);
+    e = nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, s);
     if (e != cudaSuccess) return e;
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, s);
     if (e != cudaSuccess) return e;
+    if (particles) {
+        // Targets are visited in the same Morton order, so the targets of a
+        // warp are close together and most j-tiles take the branch-free loop.
+        if (active_only) {
+            e = nb::launch_active_list(h->ti_end, h->n, h->perm, h->clk, h->active, s);
+            if (e != cudaSuccess) return e;
+            t2.idx = h->active;
+            t2.d_count = &h->clk->n_active;
+        } else {
+            t2.idx = h->perm;
+        }
+    }
     nb::Sources32 src{h->pack, h->origin, h->ntiles, kTileJ};
-    nb::Targets t2 = tg;
-    // All-particle evaluations visit the targets in the same Morton order.
-    if (!t2.idx && t2.x == h->x) t2.idx = h->perm;
     return nb::launch_force_mixed(h->p.law, pot, src, t2, h->p.G, &h->clk->err, h->block, h->ipt,
                                   s);
 }
@@ -188,14 +208,12 @@ cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
         e = nb::launch_drift(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->n, h->tc, h->clk, 0, 0, 0.0,
                              s);
         if (e != cudaSuccess) return e;
-        e = nb::launch_active_list(h->ti_end, h->n, h->clk, h->active, s);
-        if (e != cudaSuccess) return e;
     } else {
         e = nb::launch_drift(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->n, h->tc, h->clk, 2, 0, 0.0,
                              s);
         if (e != cudaSuccess) return e;
     }
-    e = enqueue_force(h, particle_targets(h, adaptive, true, false), s);
+    e = enqueue_force(h, particle_targets(h, true, false), s, adaptive);
     if (e != cudaSuccess) return e;
     e = nb::launch_kick(h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->type, h->ti_beg, h->ti_end,
                         h->n, h->tc, h->clk, s);
@@ -479,9 +497,8 @@ int nb_compute_force(nb_handle* h, int flags) {
     rc = require_particles(h);
     if (rc) return rc;
     const bool adaptive = h->p.adaptive != 0;
-    if (adaptive) NB_CK(nb::launch_active_list(h->ti_end, h->n, h->clk, h->active, h->stream));
-    NB_CK(enqueue_force(h, particle_targets(h, adaptive, true, (flags & NB_FORCE_POT) != 0),
-                        h->stream));
+    NB_CK(enqueue_force(h, particle_targets(h, true, (flags & NB_FORCE_POT) != 0), h->stream,
+                        adaptive));
     return sync_and_check(h);
 }
 
@@ -491,7 +508,7 @@ int nb_compute_potential(nb_handle* h) {
     if (rc) return rc;
     rc = require_particles(h);
     if (rc) return rc;
-    NB_CK(enqueue_force(h, particle_targets(h, false, false, true), h->stream));
+    NB_CK(enqueue_force(h, particle_targets(h, false, true), h->stream, false));
     return sync_and_check(h);
 }
 
@@ -556,7 +573,7 @@ int nb_force_at_points(nb_handle* h, int64_t n, const double* px, const double* 
     t.az = want_acc ? oaz : nullptr;
     t.pot = pot ? opot : nullptr;
     t.self_mass = nullptr;
-    NB_CK(enqueue_force(h, t, s));
+    NB_CK(enqueue_force(h, t, s, false));
     if (ax) NB_CK(cudaMemcpyAsync(ax, oax, d, cudaMemcpyDeviceToHost, s));
     if (ay) NB_CK(cudaMemcpyAsync(ay, oay, d, cudaMemcpyDeviceToHost, s));
     if (az) NB_CK(cudaMemcpyAsync(az, oaz, d, cudaMemcpyDeviceToHost, s));
@@ -682,7 +699,7 @@ int nb_diagnostics(nb_handle* h, int with_potential, nb_diag* out) {
     if (rc) return rc;
     rc = require_particles(h);
     if (rc) return rc;
-    if (with_potential) NB_CK(enqueue_force(h, particle_targets(h, false, false, true), h->stream));
+    if (with_potential) NB_CK(enqueue_force(h, particle_targets(h, false, true), h->stream, false));
     NB_CK(nb::launch_diag(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->m, h->pot, h->n,
                           h->diag_scratch, h->diag_blocks, h->diag_out, h->stream));
     double o[8];
@@ -706,7 +723,7 @@ int nb_active_count(nb_handle* h, int64_t* count) {
         *count = 0;
         return NB_OK;
     }
-    NB_CK(nb::launch_active_list(h->ti_end, h->n, h->clk, h->active, h->stream));
+    NB_CK(nb::launch_active_list(h->ti_end, h->n, nullptr, h->clk, h->active, h->stream));
     int32_t c = 0;
     NB_CK(cudaMemcpyAsync(&c, &h->clk->n_active, sizeof c, cudaMemcpyDeviceToHost, h->stream));
     NB_CK(cudaStreamSynchronize(h->stream));

@@ -135,6 +135,45 @@ __device__ __forceinline__ void spline_close(float r2, float rinv, float m, floa
 }
 
 // ---------------------------------------------------------------------------
+// Pair loop over one j-tile in shared memory for IPT targets held in
+// registers.  CHECK selects the variant that tests r < h per pair (spline slow
+// path); the unchecked variant is branch-free.
+// ---------------------------------------------------------------------------
+template <int LAW, bool ACC, bool POT, int IPT, bool CHECK>
+__device__ __forceinline__ void pair_loop(const float4* __restrict__ b, const float* xr,
+                                          const float* yr, const float* zr, const float* hh,
+                                          const float* h2, float* ax, float* ay, float* az,
+                                          float* ap) {
+#pragma unroll 4
+    for (int j = 0; j < kTileJ; ++j) {
+        const float4 q = b[j];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const float dx = q.x - xr[k];
+            const float dy = q.y - yr[k];
+            const float dz = q.z - zr[k];
+            float r2;
+            if (LAW == NB_LAW_PLUMMER)
+                r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, h2[k])));
+            else
+                r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float rinv = rsqrt_approx(r2);
+            float mp = q.w * rinv;
+            float mr3 = mp * rinv * rinv;
+            if (CHECK && LAW == NB_LAW_SPLINE_G2) {
+                if (r2 < h2[k]) spline_close(r2, rinv, q.w, hh[k], mr3, mp);
+            }
+            if (ACC) {
+                ax[k] = fmaf(dx, mr3, ax[k]);
+                ay[k] = fmaf(dy, mr3, ay[k]);
+                az[k] = fmaf(dz, mr3, az[k]);
+            }
+            if (POT) ap[k] -= mp;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Force kernel.
 // ---------------------------------------------------------------------------
 template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
@@ -212,33 +251,24 @@ __global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg
         const bool ok = mbar_wait_bounded(&full[s], par, kWaitTimeoutNs);
         if (ok) {
             const float4* b = &buf[s * kTileJ];
-#pragma unroll 4
-            for (int j = 0; j < kTileJ; ++j) {
-                const float4 q = b[j];
+            // Warp-uniform choice of the pair loop: when every target of the
+            // warp lies farther than (tile radius + h) from the tile origin, no
+            // pair of this tile can have r < h and the branch-free loop runs.
+            bool near = false;
+            if (LAW == NB_LAW_SPLINE_G2) {
+                const float R = (float)o.w;
 #pragma unroll
                 for (int k = 0; k < IPT; ++k) {
-                    const float dx = q.x - xr[k];
-                    const float dy = q.y - yr[k];
-                    const float dz = q.z - zr[k];
-                    float r2;
-                    if (LAW == NB_LAW_PLUMMER)
-                        r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, h2[k])));
-                    else
-                        r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    const float rinv = rsqrt_approx(r2);
-                    float mp = q.w * rinv;
-                    float mr3 = mp * rinv * rinv;
-                    if (LAW == NB_LAW_SPLINE_G2) {
-                        if (__builtin_expect(r2 < h2[k], 0)) spline_close(r2, rinv, q.w, hh[k], mr3, mp);
-                    }
-                    if (ACC) {
-                        ax[k] = fmaf(dx, mr3, ax[k]);
-                        ay[k] = fmaf(dy, mr3, ay[k]);
-                        az[k] = fmaf(dz, mr3, az[k]);
-                    }
-                    if (POT) ap[k] -= mp;
+                    const float d2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
+                    const float lim = (R + hh[k]) * 1.0001f;
+                    near |= (pidx[k] >= 0) && (d2 <= lim * lim);
                 }
+                near = __any_sync(0xffffffffu, near);
             }
+            if (near)
+                pair_loop<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+            else
+                pair_loop<LAW, ACC, POT, IPT, false>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
         }
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {

@@ -37,11 +37,13 @@ __device__ __forceinline__ int64_t get_timestep(double ax, double ay, double az,
 // Active list: particles with Ti_endstep == system_time_int
 // (src/directsum/gravity.jl:95-96).  Order within the list is irrelevant: each
 // target's sum runs over all sources in a fixed order.
-__global__ void k_active_list(const int64_t* __restrict__ ti_end, int64_t n, Clock* clk,
+__global__ void k_active_list(const int64_t* __restrict__ ti_end, int64_t n,
+                              const int32_t* __restrict__ perm, Clock* clk,
                               int32_t* __restrict__ list) {
-    const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    const int64_t slot = (int64_t)blockIdx.x * kBlock + threadIdx.x;
     const int64_t now = clk->t_int;
-    const bool act = i < n && ti_end[i] == now;
+    const int64_t i = slot < n ? (perm ? (int64_t)perm[slot] : slot) : 0;
+    const bool act = slot < n && ti_end[i] == now;
     const unsigned mask = __ballot_sync(0xffffffffu, act);
     const int lane = threadIdx.x & 31;
     int base = 0;
@@ -50,12 +52,12 @@ __global__ void k_active_list(const int64_t* __restrict__ ti_end, int64_t n, Clo
     if (act) list[base + __popc(mask & ((1u << lane) - 1u))] = (int32_t)i;
 }
 
-cudaError_t launch_active_list(const int64_t* ti_end, int64_t n, Clock* clk, int32_t* list,
-                               cudaStream_t s) {
+cudaError_t launch_active_list(const int64_t* ti_end, int64_t n, const int32_t* perm, Clock* clk,
+                               int32_t* list, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(&clk->n_active, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return e;
     if (n <= 0) return cudaSuccess;
-    k_active_list<<<grid_for(n), kBlock, 0, s>>>(ti_end, n, clk, list);
+    k_active_list<<<grid_for(n), kBlock, 0, s>>>(ti_end, n, perm, clk, list);
     return cudaGetLastError();
 }
 

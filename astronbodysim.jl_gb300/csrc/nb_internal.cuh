@@ -107,8 +107,10 @@ cudaError_t launch_force_fp64(int law, bool pot, const Sources64& src, const Tar
                               double G, uint32_t* err, cudaStream_t s);
 
 // Integrator kernels (nb_integrate.cu).
-cudaError_t launch_active_list(const int64_t* ti_end, int64_t n, Clock* clk, int32_t* list,
-                               cudaStream_t s);
+// Active list (Ti_endstep == t_int); slots are scanned in perm order when perm
+// is given, so consecutive list entries stay spatially close.
+cudaError_t launch_active_list(const int64_t* ti_end, int64_t n, const int32_t* perm, Clock* clk,
+                               int32_t* list, cudaStream_t s);
 cudaError_t launch_init_timesteps(const double* ax, const double* ay, const double* az,
                                   const int32_t* type, int64_t* ti_beg, int64_t* ti_end, int64_t n,
                                   TimeCfg cfg, Clock* clk, cudaStream_t s);
