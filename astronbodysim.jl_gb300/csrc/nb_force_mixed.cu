@@ -29,8 +29,11 @@ constexpr uint64_t kWaitTimeoutNs = 2000000000ull;  // 2 s
 
 // ---------------------------------------------------------------------------
 // Pack: one CTA of kTileJ threads per j-tile.  Slot i of the packed array holds
-// particle perm[i] (identity when perm == nullptr); the tile origin is the
-// centre of the tile's FP64 bounding box and origin.w its half diagonal.
+// particle perm[i] (identity when perm == nullptr), in pairs: slots 2p, 2p+1 of
+// a tile are stored as float4 (x0, x1, y0, y1), float4 (z0, z1, m0, m1), so
+// the packed-FP32x2 pair loop evaluates two sources per instruction.  The tile
+// origin is the centre of the tile's FP64 bounding box, origin.w its half
+// diagonal.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
                                                  const double* __restrict__ y,
@@ -84,15 +87,22 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
     const double ox = 0.5 * (lo[0] + hi[0]);
     const double oy = 0.5 * (lo[1] + hi[1]);
     const double oz = 0.5 * (lo[2] + hi[2]);
-    float4 q;
+    float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
     if (valid) {
-        q = make_float4((float)(px - ox), (float)(py - oy), (float)(pz - oz), (float)pm);
-    } else {
-        // Zero-mass padding far away: contributes exactly 0 and never takes the
-        // r < h path.
-        q = make_float4(1e18f, 1e18f, 1e18f, 0.0f);
+        qx = (float)(px - ox);
+        qy = (float)(py - oy);
+        qz = (float)(pz - oz);
+        qm = (float)pm;
     }
-    pack[i] = q;
+    // (Zero-mass padding far away contributes exactly 0 and never takes the
+    // r < h path.)  Paired layout: sources 2p and 2p+1 of the tile occupy
+    // float4 (x0, x1, y0, y1) and float4 (z0, z1, m0, m1).
+    float* base = reinterpret_cast<float*>(pack + (int64_t)blockIdx.x * kTileJ);
+    const int pr = threadIdx.x >> 1, half = threadIdx.x & 1;
+    base[8 * pr + half] = qx;
+    base[8 * pr + 2 + half] = qy;
+    base[8 * pr + 4 + half] = qz;
+    base[8 * pr + 6 + half] = qm;
     if (threadIdx.x == 0) {
         const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
         origin[blockIdx.x] = make_dvec4(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
@@ -131,44 +141,103 @@ __device__ __forceinline__ void spline_close(float r2, float rinv, float m, floa
              u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
     }
     mr3 = m * hinv3 * fac;
-    mp = (r2 > 0.0f) ? -(m * hinv * wp) : 0.0f;
+    mp = (r2 > 0.0f) ? -(m * hinv * wp) : 0.0f;  // +m/r convention: phi contribution is -mp
 }
 
 // ---------------------------------------------------------------------------
-// Pair loop over one j-tile in shared memory for IPT targets held in
-// registers.  CHECK selects the variant that tests r < h per pair (spline slow
-// path); the unchecked variant is branch-free.
+// Pair loops over one j-tile in shared memory (paired layout) for IPT targets
+// held in registers.
+//
+// pair_loop_fast: branch-free, packed FP32x2 arithmetic (fma/mul/add .f32x2):
+// each instruction evaluates one target against the two sources of a pair, so
+// an interaction costs 6 issue slots of FP32 math + 1 MUFU rsqrt.  Used for
+// every tile in the Plummer law and for far tiles in the spline law.
+// pair_loop_checked: scalar, tests r < h per pair (spline slow path, j == i).
+// Both accumulate per-tile partials; pot accumulates +m/r (negated later).
 // ---------------------------------------------------------------------------
-template <int LAW, bool ACC, bool POT, int IPT, bool CHECK>
-__device__ __forceinline__ void pair_loop(const float4* __restrict__ b, const float* xr,
-                                          const float* yr, const float* zr, const float* hh,
-                                          const float* h2, float* ax, float* ay, float* az,
-                                          float* ap) {
+template <int LAW, bool ACC, bool POT, int IPT>
+__device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, const float* xr,
+                                               const float* yr, const float* zr, const float* h2,
+                                               float* ax, float* ay, float* az, float* ap) {
+    float2 nx[IPT], ny[IPT], nz[IPT], e2[IPT];
+    float2 sx[IPT], sy[IPT], sz[IPT], sp[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        nx[k] = make_float2(-xr[k], -xr[k]);
+        ny[k] = make_float2(-yr[k], -yr[k]);
+        nz[k] = make_float2(-zr[k], -zr[k]);
+        e2[k] = make_float2(h2[k], h2[k]);
+        sx[k] = sy[k] = sz[k] = sp[k] = make_float2(0.0f, 0.0f);
+    }
 #pragma unroll 4
-    for (int j = 0; j < kTileJ; ++j) {
-        const float4 q = b[j];
+    for (int p = 0; p < kTileJ / 2; ++p) {
+        const float4 A = b[2 * p];
+        const float4 B = b[2 * p + 1];
+        const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+        const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
-            const float dx = q.x - xr[k];
-            const float dy = q.y - yr[k];
-            const float dz = q.z - zr[k];
-            float r2;
-            if (LAW == NB_LAW_PLUMMER)
-                r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, h2[k])));
-            else
-                r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float rinv = rsqrt_approx(r2);
-            float mp = q.w * rinv;
-            float mr3 = mp * rinv * rinv;
-            if (CHECK && LAW == NB_LAW_SPLINE_G2) {
-                if (r2 < h2[k]) spline_close(r2, rinv, q.w, hh[k], mr3, mp);
-            }
+            const float2 dx = __fadd2_rn(qx, nx[k]);
+            const float2 dy = __fadd2_rn(qy, ny[k]);
+            const float2 dz = __fadd2_rn(qz, nz[k]);
+            float2 r2 = (LAW == NB_LAW_PLUMMER) ? __ffma2_rn(dz, dz, e2[k]) : __fmul2_rn(dz, dz);
+            r2 = __ffma2_rn(dy, dy, r2);
+            r2 = __ffma2_rn(dx, dx, r2);
+            const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+            const float2 mp = __fmul2_rn(qm, rinv);
             if (ACC) {
-                ax[k] = fmaf(dx, mr3, ax[k]);
-                ay[k] = fmaf(dy, mr3, ay[k]);
-                az[k] = fmaf(dz, mr3, az[k]);
+                const float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
+                sx[k] = __ffma2_rn(dx, mr3, sx[k]);
+                sy[k] = __ffma2_rn(dy, mr3, sy[k]);
+                sz[k] = __ffma2_rn(dz, mr3, sz[k]);
             }
-            if (POT) ap[k] -= mp;
+            if (POT) sp[k] = __fadd2_rn(sp[k], mp);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        ax[k] += sx[k].x + sx[k].y;
+        ay[k] += sy[k].x + sy[k].y;
+        az[k] += sz[k].x + sz[k].y;
+        ap[k] += sp[k].x + sp[k].y;
+    }
+}
+
+template <int LAW, bool ACC, bool POT, int IPT>
+__device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, const float* xr,
+                                                  const float* yr, const float* zr,
+                                                  const float* hh, const float* h2, float* ax,
+                                                  float* ay, float* az, float* ap) {
+#pragma unroll 2
+    for (int p = 0; p < kTileJ / 2; ++p) {
+        const float4 A = b[2 * p];
+        const float4 B = b[2 * p + 1];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const float4 q = half ? make_float4(A.y, A.w, B.y, B.w) : make_float4(A.x, A.z, B.x, B.z);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float dx = q.x - xr[k];
+                const float dy = q.y - yr[k];
+                const float dz = q.z - zr[k];
+                float r2;
+                if (LAW == NB_LAW_PLUMMER)
+                    r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, h2[k])));
+                else
+                    r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const float rinv = rsqrt_approx(r2);
+                float mp = q.w * rinv;
+                float mr3 = mp * rinv * rinv;
+                if (LAW == NB_LAW_SPLINE_G2) {
+                    if (r2 < h2[k]) spline_close(r2, rinv, q.w, hh[k], mr3, mp);
+                }
+                if (ACC) {
+                    ax[k] = fmaf(dx, mr3, ax[k]);
+                    ay[k] = fmaf(dy, mr3, ay[k]);
+                    az[k] = fmaf(dz, mr3, az[k]);
+                }
+                if (POT) ap[k] += mp;
+            }
         }
     }
 }
@@ -266,9 +335,9 @@ __global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg
                 near = __any_sync(0xffffffffu, near);
             }
             if (near)
-                pair_loop<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
             else
-                pair_loop<LAW, ACC, POT, IPT, false>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+                pair_loop_fast<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap);
         }
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
@@ -306,7 +375,8 @@ __global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg
             tg.az[p] = ((double)sz[k] + (double)cz[k]) * G;
         }
         if (POT) {
-            double phi = (double)sp[k] + (double)cp[k];
+            // The loops accumulate +m/r; phi = -sum.
+            double phi = -((double)sp[k] + (double)cp[k]);
             if (LAW == NB_LAW_PLUMMER && tg.self_mass) {
                 // Remove the self pair, bit-identical to the term the loop added.
                 const float mself = (float)tg.self_mass[p];
