@@ -24,7 +24,7 @@
 namespace nb {
 
 constexpr int kTileJ = 256;
-constexpr int kStages = 3;
+constexpr int kStages = 4;
 constexpr uint64_t kWaitTimeoutNs = 2000000000ull;  // 2 s
 
 // ---------------------------------------------------------------------------
@@ -244,23 +244,66 @@ __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, 
 
 // ---------------------------------------------------------------------------
 // Force kernel.
+//
+// CTA = BLOCK threads, IPT targets per thread (slot k*BLOCK + tid).  Targets'
+// FP64 positions live in shared memory; per j-tile each thread re-expresses
+// them relative to the tile origin in FP64 and rounds to FP32.
+//
+// j-tiles stream through a kStages ring.  full[s] (mbarrier, count 1 +
+// transaction bytes) completes when the bulk copy of the tile has landed.
+// There is no CTA-wide barrier per tile: every warp bumps done[s] after it has
+// read stage s, and the last warp to do so re-arms full[s] and issues the copy
+// of tile t + kStages into it.  Warps may therefore run up to kStages - 1
+// tiles apart.  Every wait is bounded; a timed-out warp records
+// DEVERR_TIMEOUT and stops, and the CTA drains its copies before exiting.
 // ---------------------------------------------------------------------------
 template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg, double G,
+__global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 : 1) k_force_mixed(Sources32 src, Targets tg, double G,
                                                        uint32_t* __restrict__ err) {
+    constexpr int kWarpsPerCta = BLOCK / 32;
     __shared__ __align__(128) float4 buf[kStages * kTileJ];
     __shared__ __align__(8) uint64_t full[kStages];
+    __shared__ uint32_t done[kStages];
+    __shared__ uint32_t abort_flag;
+    __shared__ double tpx[BLOCK * IPT], tpy[BLOCK * IPT], tpz[BLOCK * IPT];
 
     const int64_t ntg = tg.d_count ? (int64_t)(*tg.d_count) : tg.n;
     const int64_t base = (int64_t)blockIdx.x * (BLOCK * IPT);
     if (base >= ntg) return;  // CTA-uniform
     const int tid = threadIdx.x;
+    const int lane = tid & 31;
     const int ntiles = src.ntiles;
 
     if (tid == 0) {
 #pragma unroll
-        for (int s = 0; s < kStages; ++s) mbar_init(&full[s], 1);
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            done[s] = 0;
+        }
+        abort_flag = 0;
         fence_mbar_init();
+    }
+
+    int32_t pidx[IPT];
+    float hh[IPT], h2[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int64_t t = base + k * BLOCK + tid;
+        pidx[k] = -1;
+        double x = 0.0, y = 0.0, z = 0.0, h = tg.h_const;
+        if (t < ntg) {
+            const int32_t p = tg.idx ? tg.idx[t] : (int32_t)t;
+            pidx[k] = p;
+            x = tg.x[p];
+            y = tg.y[p];
+            z = tg.z[p];
+            if (tg.type) h = tg.soft[tg.type[p] - 1];
+        }
+        tpx[k * BLOCK + tid] = x;
+        tpy[k * BLOCK + tid] = y;
+        tpz[k * BLOCK + tid] = z;
+        hh[k] = (float)h;
+        h2[k] = hh[k] * hh[k];
     }
     __syncthreads();
     if (tid == 0) {
@@ -271,29 +314,6 @@ __global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg
         }
     }
 
-    int32_t pidx[IPT];
-    double px[IPT], py[IPT], pz[IPT];
-    float hh[IPT], h2[IPT];
-#pragma unroll
-    for (int k = 0; k < IPT; ++k) {
-        const int64_t t = base + k * BLOCK + tid;
-        pidx[k] = -1;
-        px[k] = 0.0;
-        py[k] = 0.0;
-        pz[k] = 0.0;
-        double h = tg.h_const;
-        if (t < ntg) {
-            const int32_t p = tg.idx ? tg.idx[t] : (int32_t)t;
-            pidx[k] = p;
-            px[k] = tg.x[p];
-            py[k] = tg.y[p];
-            pz[k] = tg.z[p];
-            if (tg.type) h = tg.soft[tg.type[p] - 1];
-        }
-        hh[k] = (float)h;
-        h2[k] = hh[k] * hh[k];
-    }
-
     float sx[IPT], sy[IPT], sz[IPT], sp[IPT];
     float cx[IPT], cy[IPT], cz[IPT], cp[IPT];
 #pragma unroll
@@ -302,6 +322,7 @@ __global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg
         cx[k] = cy[k] = cz[k] = cp[k] = 0.0f;
     }
 
+    bool timed_out = false;
     for (int t = 0; t < ntiles; ++t) {
         const int s = t % kStages;
         const uint32_t par = (uint32_t)(t / kStages) & 1u;
@@ -309,35 +330,57 @@ __global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg
         float xr[IPT], yr[IPT], zr[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
-            xr[k] = (float)(px[k] - o.x);
-            yr[k] = (float)(py[k] - o.y);
-            zr[k] = (float)(pz[k] - o.z);
+            xr[k] = (float)(tpx[k * BLOCK + tid] - o.x);
+            yr[k] = (float)(tpy[k * BLOCK + tid] - o.y);
+            zr[k] = (float)(tpz[k * BLOCK + tid] - o.z);
         }
         float ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = ap[k] = 0.0f;
 
-        const bool ok = mbar_wait_bounded(&full[s], par, kWaitTimeoutNs);
-        if (ok) {
-            const float4* b = &buf[s * kTileJ];
-            // Warp-uniform choice of the pair loop: when every target of the
-            // warp lies farther than (tile radius + h) from the tile origin, no
-            // pair of this tile can have r < h and the branch-free loop runs.
-            bool near = false;
-            if (LAW == NB_LAW_SPLINE_G2) {
-                const float R = (float)o.w;
-#pragma unroll
-                for (int k = 0; k < IPT; ++k) {
-                    const float d2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
-                    const float lim = (R + hh[k]) * 1.0001f;
-                    near |= (pidx[k] >= 0) && (d2 <= lim * lim);
-                }
-                near = __any_sync(0xffffffffu, near);
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], par, kWaitTimeoutNs));
+        if (!ok || abort_flag) {
+            timed_out = true;
+            if (lane == 0) {
+                atomicOr(err, DEVERR_TIMEOUT);
+                atomicExch(&abort_flag, 1u);
             }
-            if (near)
-                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
-            else
-                pair_loop_fast<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap);
+            break;
+        }
+        const float4* b = &buf[s * kTileJ];
+        // Warp-uniform choice of the pair loop: when every target of the warp
+        // lies farther than (tile radius + h) from the tile origin, no pair of
+        // this tile can have r < h and the branch-free loop runs.
+        bool near = false;
+        if (LAW == NB_LAW_SPLINE_G2) {
+            const float R = (float)o.w;
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float d2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
+                const float lim = (R + hh[k]) * 1.0001f;
+                near |= (pidx[k] >= 0) && (d2 <= lim * lim);
+            }
+            near = __any_sync(0xffffffffu, near);
+        }
+        if (near)
+            pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+        else
+            pair_loop_fast<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap);
+
+        // Release stage s; the last warp out refills it with tile t + kStages.
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            const uint32_t prev = atomicAdd(&done[s], 1u);
+            if (prev == kWarpsPerCta - 1) {
+                __threadfence_block();
+                done[s] = 0;
+                if (t + kStages < ntiles) {
+                    mbar_arrive_expect_tx(&full[s], kTileJ * sizeof(float4));
+                    bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)(t + kStages) * kTileJ,
+                             kTileJ * sizeof(float4), &full[s]);
+                }
+            }
         }
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
@@ -348,21 +391,16 @@ __global__ void __launch_bounds__(BLOCK) k_force_mixed(Sources32 src, Targets tg
             }
             if (POT) two_sum_acc(sp[k], cp[k], ap[k]);
         }
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                atomicOr(err, DEVERR_TIMEOUT);
-                // Drain the copies this CTA still has in flight before exiting.
-                for (int u = t; u < t + kStages && u < ntiles; ++u)
-                    (void)mbar_wait_bounded(&full[u % kStages], (uint32_t)(u / kStages) & 1u,
-                                            kWaitTimeoutNs);
-            }
-            return;
+    }
+
+    if (__syncthreads_or(timed_out)) {
+        if (tid == 0) {
+            // Drain every copy that may still be in flight before exiting.
+            for (int u = 0; u < ntiles; ++u)
+                (void)mbar_wait_bounded(&full[u % kStages], (uint32_t)(u / kStages) & 1u,
+                                        kWaitTimeoutNs / 8);
         }
-        if (tid == 0 && t + kStages < ntiles) {
-            mbar_arrive_expect_tx(&full[s], kTileJ * sizeof(float4));
-            bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)(t + kStages) * kTileJ,
-                     kTileJ * sizeof(float4), &full[s]);
-        }
+        return;
     }
 
 #pragma unroll
