@@ -108,6 +108,9 @@ SIGNATURES = {
     "nb_get_time": (ctypes.c_int, [_h, _i64p, _dp]),
     "nb_diagnostics": (ctypes.c_int, [_h, ctypes.c_int, ctypes.POINTER(nb_diag)]),
     "nb_active_count": (ctypes.c_int, [_h, _i64p]),
+    "nb_force_noalloc": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int32,
+                                        ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp,
+                                        ctypes.c_char_p, ctypes.c_int64]),
     "nb_last_error": (ctypes.c_char_p, [_h]),
     "nb_version": (ctypes.c_char_p, []),
 }

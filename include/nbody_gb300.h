@@ -174,6 +174,27 @@ int nb_diagnostics(nb_handle *h, int with_potential, nb_diag *out);
 /* Number of particles active at the current time (Ti_endstep == t_int). */
 int nb_active_count(nb_handle *h, int64_t *count);
 
+/* Mixed-precision acceleration (and, if pot != NULL, potential per unit mass)
+ * of n particles from the same n particles, one softening length for all,
+ * without allocating any device memory.  No counterpart in the reference: it
+ * exists for callers that cannot let the library call cudaMalloc -- a Julia
+ * host whose device arrays all come from CUDA.jl's pooled allocator, or a
+ * serving process that reserves its HBM budget up front.  x, y, z, m, ax, ay,
+ * az, pot are device pointers of the caller on the current device; stream is
+ * a cudaStream_t (NULL = legacy default stream); the call synchronises the
+ * stream before returning.  Scratch is one fixed device array of this library
+ * (about 2.7 MB, held by every GPU that loads the library until exit), so
+ * n must be 1..65536; larger n returns NB_ERR_INVALID_ARG with a message in
+ * errbuf (may be NULL).  All calls share that array: calls that overlap on the
+ * GPU race and must be serialised by the caller.  The first call on a device
+ * looks up the array's address and should come before any stream capture.
+ * Results equal nb_compute_force of a handle with NB_PREC_MIXED, the same law,
+ * G and softening for every particle type. */
+int nb_force_noalloc(int64_t n, const double *x, const double *y, const double *z,
+                     const double *m, int32_t law, double G, double softening, double *ax,
+                     double *ay, double *az, double *pot, void *stream, char *errbuf,
+                     int64_t errbuf_len);
+
 /* Last error message of this handle (never NULL). */
 const char *nb_last_error(nb_handle *h);
 
