@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -31,6 +32,7 @@ struct nb_handle {
     int64_t *ti_beg = nullptr, *ti_end = nullptr;
     int32_t* active = nullptr;
     int32_t* perm = nullptr;
+    uint32_t* act_scratch = nullptr;
     void* sort_scratch = nullptr;
     float4* pack = nullptr;
     nb::dvec4* origin = nullptr;
@@ -44,6 +46,14 @@ struct nb_handle {
     cudaGraphExec_t step_exec = nullptr;
     int block = 128;
     int ipt = 2;
+    bool worklist = false;     // persistent work-list kernel forced (block == -1)
+    bool auto_cfg = true;      // kernel and shape chosen per N
+    int wl_mode = 0;           // 0: even unit split, 1: block-cyclic whole blocks
+    int nsm = 0;
+    int wl_occ[2][3] = {};     // CTAs per SM of k_force_worklist [law][acc, acc+pot, pot]
+    nb::SysDesc* sysdesc = nullptr;
+    float* partial = nullptr;
+    size_t partial_bytes = 0;
     std::string err;
 };
 
@@ -108,7 +118,8 @@ int check_params(nb_handle* h, const nb_params* p) {
         if (!(p->eta > 0.0)) return fail(h, NB_ERR_INVALID_ARG, "eta must be > 0");
     }
     const int b = p->block, i = p->i_per_thread;
-    if (b != 0 && b != 128 && b != 256) return fail(h, NB_ERR_INVALID_ARG, "block must be 128 or 256");
+    if (b != 0 && b != -1 && b != 128 && b != 256)
+        return fail(h, NB_ERR_INVALID_ARG, "block must be 0 (auto), -1 (work list), 128 or 256");
     if (i != 0 && i != 1 && i != 2 && i != 4)
         return fail(h, NB_ERR_INVALID_ARG, "i_per_thread must be 1, 2 or 4");
     if (p->tile_j != 0 && p->tile_j != kTileJ)
@@ -167,7 +178,7 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     cudaError_t e;
     if (h->p.precision == NB_PREC_FP64) {
         if (active_only) {
-            e = nb::launch_active_list(h->ti_end, h->n, nullptr, h->clk, h->active, s);
+            e = nb::launch_active_list(h->ti_end, h->n, nullptr, h->clk, h->active, h->act_scratch, s);
             if (e != cudaSuccess) return e;
             t2.idx = h->active;
             t2.d_count = &h->clk->n_active;
@@ -181,11 +192,58 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     if (e != cudaSuccess) return e;
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, s);
     if (e != cudaSuccess) return e;
+    // Measured on GB300 (Plummer, spline): the direct grid with one target per
+    // thread is fastest from N = 2^19 up; below, the evenly split work list
+    // avoids the partial last wave of the direct grid.
+    bool use_wl = h->worklist;
+    int blk = h->block, ipt = h->ipt;
+    if (h->auto_cfg) {
+        use_wl = h->n < (int64_t(1) << 19);
+        blk = 128;
+        ipt = 1;
+    }
+    if (particles && use_wl) {
+        if (active_only) {
+            e = nb::launch_active_list(h->ti_end, h->n, h->perm, h->clk, h->active, h->act_scratch, s);
+            if (e != cudaSuccess) return e;
+        }
+        const bool acc = tg.ax != nullptr;
+        const int variant = acc ? (pot ? 1 : 0) : 2;
+        const int64_t bt = nb::worklist_block_targets();
+        const int64_t nblocks = (h->n + bt - 1) / bt;
+        nb::WorkList w{};
+        w.sys = h->sysdesc;
+        w.nsys = 1;
+        w.units = nblocks * (int64_t)h->ntiles;
+        int64_t grid = (int64_t)h->wl_occ[h->p.law][variant] * h->nsm;
+        w.block_cyclic = h->wl_mode == 1 ? 1 : 0;
+        if (!active_only && grid > (w.block_cyclic ? nblocks : w.units))
+            grid = w.block_cyclic ? nblocks : w.units;
+        w.grid = (int32_t)grid;
+        w.active = active_only ? h->active : nullptr;
+        w.d_count = active_only ? &h->clk->n_active : nullptr;
+        w.perm = active_only ? nullptr : h->perm;
+        w.pack = h->pack;
+        w.origin = h->origin;
+        w.x = h->x;
+        w.y = h->y;
+        w.z = h->z;
+        w.m = h->m;
+        w.type = h->type;
+        w.ax = tg.ax;
+        w.ay = tg.ay;
+        w.az = tg.az;
+        w.pot = tg.pot;
+        w.partial = h->partial;
+        w.G = h->p.G;
+        w.err = &h->clk->err;
+        return nb::launch_force_worklist(h->p.law, w, s);
+    }
     if (particles) {
         // Targets are visited in the same Morton order, so the targets of a
         // warp are close together and most j-tiles take the branch-free loop.
         if (active_only) {
-            e = nb::launch_active_list(h->ti_end, h->n, h->perm, h->clk, h->active, s);
+            e = nb::launch_active_list(h->ti_end, h->n, h->perm, h->clk, h->active, h->act_scratch, s);
             if (e != cudaSuccess) return e;
             t2.idx = h->active;
             t2.d_count = &h->clk->n_active;
@@ -194,8 +252,7 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
         }
     }
     nb::Sources32 src{h->pack, h->origin, h->ntiles, kTileJ};
-    return nb::launch_force_mixed(h->p.law, pot, src, t2, h->p.G, &h->clk->err, h->block, h->ipt,
-                                  s);
+    return nb::launch_force_mixed(h->p.law, pot, src, t2, h->p.G, &h->clk->err, blk, ipt, s);
 }
 
 // Enqueue step(sim, DirectSum, GPU): drift -> force(active) -> kick.
@@ -246,6 +303,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     size_t o_tb = take(sizeof(int64_t) * (size_t)n), o_te = take(sizeof(int64_t) * (size_t)n);
     size_t o_act = take(sizeof(int32_t) * (size_t)n);
     size_t o_perm = take(sizeof(int32_t) * (size_t)n);
+    size_t o_acts = take(sizeof(uint32_t) * (size_t)nb::active_scratch_words(n));
     size_t o_sort = take(nb::sort_scratch_bytes(n));
     size_t o_pack = take(sizeof(float4) * (size_t)npad);
     size_t o_orig = take(sizeof(nb::dvec4) * (size_t)ntiles);
@@ -272,6 +330,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->ti_end = (int64_t*)(b + o_te);
     h->active = (int32_t*)(b + o_act);
     h->perm = (int32_t*)(b + o_perm);
+    h->act_scratch = (uint32_t*)(b + o_acts);
     h->sort_scratch = (void*)(b + o_sort);
     h->pack = (float4*)(b + o_pack);
     h->origin = (nb::dvec4*)(b + o_orig);
@@ -279,6 +338,22 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->diag_blocks = dblocks / 8;
     h->diag_out = (double*)(b + o_do);
     h->ntiles = (int32_t)ntiles;
+    return NB_OK;
+}
+
+// The single-system descriptor of the work-list force (particles, tiles,
+// softening table).
+int upload_sysdesc(nb_handle* h) {
+    nb::SysDesc d{};
+    const int64_t bt = nb::worklist_block_targets();
+    d.off = 0;
+    d.ubase = 0;
+    d.n = (int32_t)h->n;
+    d.tile_off = 0;
+    d.ntiles = h->ntiles;
+    d.nblocks = (int32_t)((h->n + bt - 1) / bt);
+    for (int k = 0; k < 6; ++k) d.soft[k] = h->p.softening[k];
+    NB_CK(cudaMemcpy(h->sysdesc, &d, sizeof d, cudaMemcpyHostToDevice));
     return NB_OK;
 }
 
@@ -349,6 +424,40 @@ int nb_create(const nb_params* p, nb_handle** out) {
     c.t_float = p->time_begin;
     c.last_t_float = p->time_begin;
     cudaMemcpy(h->clk, &c, sizeof c, cudaMemcpyHostToDevice);
+    // Work-list force: persistent grid = CTAs per SM x SMs for each variant;
+    // the partial-sum scratch is sized for the largest grid.
+    // block == -1: persistent work-list kernel; block/ipt given: direct grid with
+    // that shape; 0/0: chosen per particle count in enqueue_force.
+    h->worklist = p->block == -1;
+    h->auto_cfg = p->block == 0 && p->i_per_thread == 0;
+    if (p->block == -1) h->block = 128;
+    cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->dev);
+    int occ_max = 0;
+    for (int law = 0; law < 2; ++law)
+        for (int v = 0; v < 3; ++v) {
+            h->wl_occ[law][v] = nb::worklist_ctas_per_sm(law, v != 2, v != 0);
+            if (h->wl_occ[law][v] < 1) h->wl_occ[law][v] = 1;
+            if (h->wl_occ[law][v] > occ_max) occ_max = h->wl_occ[law][v];
+        }
+    if (const char* ev = std::getenv("NBODY_GB300_WL_MODE")) h->wl_mode = std::atoi(ev) == 1 ? 1 : 0;
+    // Tuning override: CTAs per SM of the persistent work-list grid.
+    if (const char* ev = std::getenv("NBODY_GB300_WL_CTAS_PER_SM")) {
+        const int o = std::atoi(ev);
+        if (o >= 1 && o <= 32) {
+            for (int law = 0; law < 2; ++law)
+                for (int v = 0; v < 3; ++v) h->wl_occ[law][v] = o;
+            if (o > occ_max) occ_max = o;
+        }
+    }
+    h->partial_bytes = nb::worklist_partial_bytes((int64_t)occ_max * h->nsm);
+    if (cudaMalloc(&h->partial, h->partial_bytes) != cudaSuccess ||
+        cudaMalloc(&h->sysdesc, sizeof(nb::SysDesc)) != cudaSuccess) {
+        if (h->partial) cudaFree(h->partial);
+        cudaFree(h->clk);
+        cudaStreamDestroy(h->own_stream);
+        delete h;
+        return NB_ERR_OOM;
+    }
     *out = h;
     return NB_OK;
 }
@@ -361,6 +470,8 @@ int nb_destroy(nb_handle* h) {
     if (h->arena) cudaFree(h->arena);
     if (h->probe) cudaFree(h->probe);
     if (h->clk) cudaFree(h->clk);
+    if (h->partial) cudaFree(h->partial);
+    if (h->sysdesc) cudaFree(h->sysdesc);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return NB_OK;
@@ -425,7 +536,7 @@ int nb_upload(nb_handle* h, int64_t n, const double* x, const double* y, const d
     c.last_t_float = h->p.time_begin;
     NB_CK(cudaMemcpyAsync(h->clk, &c, sizeof c, cudaMemcpyHostToDevice, s));
     NB_CK(cudaStreamSynchronize(s));
-    return NB_OK;
+    return upload_sysdesc(h);
 }
 
 int nb_download(nb_handle* h, double* x, double* y, double* z, double* vx, double* vy, double* vz,
@@ -487,6 +598,11 @@ int nb_set_softening(nb_handle* h, const double soft[6]) {
     for (int k = 0; k < 6; ++k) h->p.softening[k] = soft[k];
     h->tc = make_timecfg(h->p);
     drop_graph(h);
+    if (h->n > 0) {
+        int rc = use_device(h);
+        if (rc) return rc;
+        return upload_sysdesc(h);
+    }
     return NB_OK;
 }
 
@@ -723,7 +839,7 @@ int nb_active_count(nb_handle* h, int64_t* count) {
         *count = 0;
         return NB_OK;
     }
-    NB_CK(nb::launch_active_list(h->ti_end, h->n, nullptr, h->clk, h->active, h->stream));
+    NB_CK(nb::launch_active_list(h->ti_end, h->n, nullptr, h->clk, h->active, h->act_scratch, h->stream));
     int32_t c = 0;
     NB_CK(cudaMemcpyAsync(&c, &h->clk->n_active, sizeof c, cudaMemcpyDeviceToHost, h->stream));
     NB_CK(cudaStreamSynchronize(h->stream));

@@ -35,29 +35,61 @@ __device__ __forceinline__ int64_t get_timestep(double ax, double ay, double az,
 }
 
 // Active list: particles with Ti_endstep == system_time_int
-// (src/directsum/gravity.jl:95-96).  Order within the list is irrelevant: each
-// target's sum runs over all sources in a fixed order.
-__global__ void k_active_list(const int64_t* __restrict__ ti_end, int64_t n,
-                              const int32_t* __restrict__ perm, Clock* clk,
-                              int32_t* __restrict__ list) {
-    const int64_t slot = (int64_t)blockIdx.x * kBlock + threadIdx.x;
-    const int64_t now = clk->t_int;
-    const int64_t i = slot < n ? (perm ? (int64_t)perm[slot] : slot) : 0;
-    const bool act = slot < n && ti_end[i] == now;
-    const unsigned mask = __ballot_sync(0xffffffffu, act);
-    const int lane = threadIdx.x & 31;
-    int base = 0;
-    if (lane == 0 && mask) base = atomicAdd(&clk->n_active, __popc(mask));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (act) list[base + __popc(mask & ((1u << lane) - 1u))] = (int32_t)i;
+// (src/directsum/gravity.jl:95-96), compacted in slot order (perm order when
+// perm is given) by count -> exclusive scan -> scatter, so the list is the
+// same on every run and consecutive entries are spatially close.
+__device__ __forceinline__ bool slot_active(const int64_t* __restrict__ ti_end, int64_t n,
+                                            const int32_t* __restrict__ perm, int64_t now,
+                                            int64_t slot, int32_t& i) {
+    i = 0;
+    if (slot >= n) return false;
+    i = perm ? perm[slot] : (int32_t)slot;
+    return ti_end[i] == now;
 }
 
+__global__ void __launch_bounds__(kBlock) k_active_count(const int64_t* __restrict__ ti_end,
+                                                         int64_t n, const int32_t* __restrict__ perm,
+                                                         const Clock* __restrict__ clk,
+                                                         uint32_t* __restrict__ counts) {
+    int32_t i;
+    const bool act = slot_active(ti_end, n, perm, clk->t_int,
+                                 (int64_t)blockIdx.x * kBlock + threadIdx.x, i);
+    const int c = __syncthreads_count(act);
+    if (threadIdx.x == 0) counts[blockIdx.x] = (uint32_t)c;
+}
+
+__global__ void __launch_bounds__(kBlock) k_active_scatter(const int64_t* __restrict__ ti_end,
+                                                           int64_t n, const int32_t* __restrict__ perm,
+                                                           Clock* clk, const uint32_t* __restrict__ offs,
+                                                           int32_t* __restrict__ list) {
+    __shared__ uint32_t wcount[kBlock / 32];
+    int32_t i;
+    const bool act = slot_active(ti_end, n, perm, clk->t_int,
+                                 (int64_t)blockIdx.x * kBlock + threadIdx.x, i);
+    const unsigned mask = __ballot_sync(0xffffffffu, act);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wcount[warp] = __popc(mask);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < kBlock / 32; ++w) {
+        if (w < warp) before += wcount[w];
+        total += wcount[w];
+    }
+    const uint32_t base = offs[blockIdx.x];
+    if (act) list[base + before + __popc(mask & ((1u << lane) - 1u))] = i;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) clk->n_active = (int32_t)(base + total);
+}
+
+int64_t active_scratch_words(int64_t n) { return (n + kBlock - 1) / kBlock + 1; }
+
 cudaError_t launch_active_list(const int64_t* ti_end, int64_t n, const int32_t* perm, Clock* clk,
-                               int32_t* list, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(&clk->n_active, 0, sizeof(int32_t), s);
+                               int32_t* list, uint32_t* scratch, cudaStream_t s) {
+    if (n <= 0) return cudaMemsetAsync(&clk->n_active, 0, sizeof(int32_t), s);
+    const unsigned g = grid_for(n);
+    k_active_count<<<g, kBlock, 0, s>>>(ti_end, n, perm, clk, scratch);
+    cudaError_t e = launch_exclusive_scan(scratch, (int64_t)g, s);
     if (e != cudaSuccess) return e;
-    if (n <= 0) return cudaSuccess;
-    k_active_list<<<grid_for(n), kBlock, 0, s>>>(ti_end, n, perm, clk, list);
+    k_active_scatter<<<g, kBlock, 0, s>>>(ti_end, n, perm, clk, scratch, list);
     return cudaGetLastError();
 }
 

@@ -92,6 +92,49 @@ struct Sources64 {
     int64_t n;
 };
 
+// One independent system of a work-list force evaluation (device memory).
+struct SysDesc {
+    int64_t off;       // first particle: index into the SoA arrays and into perm
+    int64_t ubase;     // first work unit of the system
+    int32_t n;         // particles (targets and sources)
+    int32_t tile_off;  // first packed j-tile
+    int32_t ntiles;    // ceil(n / 256) j-tiles
+    int32_t nblocks;   // ceil(n / 256) i-blocks of targets
+    double soft[6];    // softening by particle type
+};
+
+// Persistent work-list force over nsys systems (nb_force_worklist.cu).
+struct WorkList {
+    const SysDesc* sys;
+    int32_t nsys;
+    int32_t grid;              // persistent CTAs; also the fix-up's partition
+    int64_t units;             // sum over systems of nblocks * ntiles
+    const int32_t* active;     // one system only: targets = active[0 .. *d_count)
+    const int32_t* d_count;
+    const int32_t* perm;       // otherwise target slot q of system s is particle perm[off + q]
+    const float4* pack;
+    const dvec4* origin;
+    const double* x;
+    const double* y;
+    const double* z;
+    const double* m;
+    const int32_t* type;       // nullptr -> soft[0]
+    double* ax;                // nullptr -> potential only
+    double* ay;
+    double* az;
+    double* pot;               // nullptr -> no potential
+    float* partial;            // worklist_partial_bytes(grid)
+    double G;
+    uint32_t* err;
+    int32_t block_cyclic;      // one system: CTA c takes whole i-blocks c, c + grid, ...
+    int32_t pad;
+};
+
+cudaError_t launch_force_worklist(int law, const WorkList& w, cudaStream_t s);
+int worklist_ctas_per_sm(int law, bool acc, bool pot);
+size_t worklist_partial_bytes(int64_t grid);
+int worklist_block_targets();
+
 // Launch helpers implemented in the .cu files.
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
                         int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
@@ -110,7 +153,9 @@ cudaError_t launch_force_fp64(int law, bool pot, const Sources64& src, const Tar
 // Active list (Ti_endstep == t_int); slots are scanned in perm order when perm
 // is given, so consecutive list entries stay spatially close.
 cudaError_t launch_active_list(const int64_t* ti_end, int64_t n, const int32_t* perm, Clock* clk,
-                               int32_t* list, cudaStream_t s);
+                               int32_t* list, uint32_t* scratch, cudaStream_t s);
+int64_t active_scratch_words(int64_t n);
+cudaError_t launch_exclusive_scan(uint32_t* counts, int64_t len, cudaStream_t s);
 cudaError_t launch_init_timesteps(const double* ax, const double* ay, const double* az,
                                   const int32_t* type, int64_t* ti_beg, int64_t* ti_end, int64_t n,
                                   TimeCfg cfg, Clock* clk, cudaStream_t s);

@@ -1,0 +1,137 @@
+// nb_pairs.cuh -- the FP32 pair arithmetic shared by the mixed-precision force
+// kernels: tile geometry, the Gadget-2 spline slow path and the two pair loops
+// over one j-tile in shared memory.
+#pragma once
+
+#include "nb_internal.cuh"
+
+namespace nb {
+
+constexpr int kTileJ = 256;
+constexpr int kStages = 4;
+constexpr uint64_t kWaitTimeoutNs = 2000000000ull;  // 2 s
+
+// ---------------------------------------------------------------------------
+// Spline slow path (r < h), FP32.  Returns m*fac (to multiply d) in mr3 and the
+// negated potential contribution in mp.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void spline_close(float r2, float rinv, float m, float h, float& mr3,
+                                             float& mp) {
+    const float hinv = 1.0f / h;
+    const float hinv3 = hinv * hinv * hinv;
+    const float r = (r2 > 0.0f) ? r2 * rinv : 0.0f;
+    const float u = r * hinv;
+    float fac, wp;
+    if (u < 0.5f) {
+        fac = 10.666666666667f + u * u * (32.0f * u - 38.4f);
+        wp = -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f));
+    } else {
+        const float u3 = u * u * u;
+        fac = 21.333333333333f - 48.0f * u + 38.4f * u * u - 10.666666666667f * u3 -
+              0.066666666667f / u3;
+        wp = -3.2f + 0.066666666667f / u +
+             u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
+    }
+    mr3 = m * hinv3 * fac;
+    mp = (r2 > 0.0f) ? -(m * hinv * wp) : 0.0f;  // +m/r convention: phi contribution is -mp
+}
+
+// ---------------------------------------------------------------------------
+// Pair loops over one j-tile in shared memory (paired layout) for IPT targets
+// held in registers.
+//
+// pair_loop_fast: branch-free, packed FP32x2 arithmetic (fma/mul/add .f32x2):
+// each instruction evaluates one target against the two sources of a pair, so
+// an interaction costs 6 issue slots of FP32 math + 1 MUFU rsqrt.  Used for
+// every tile in the Plummer law and for far tiles in the spline law.
+// pair_loop_checked: scalar, tests r < h per pair (spline slow path, j == i).
+// Both accumulate per-tile partials; pot accumulates +m/r (negated later).
+// ---------------------------------------------------------------------------
+template <int LAW, bool ACC, bool POT, int IPT>
+__device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, const float* xr,
+                                               const float* yr, const float* zr, const float* h2,
+                                               float* ax, float* ay, float* az, float* ap) {
+    float2 nx[IPT], ny[IPT], nz[IPT], e2[IPT];
+    float2 sx[IPT], sy[IPT], sz[IPT], sp[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        nx[k] = make_float2(-xr[k], -xr[k]);
+        ny[k] = make_float2(-yr[k], -yr[k]);
+        nz[k] = make_float2(-zr[k], -zr[k]);
+        e2[k] = make_float2(h2[k], h2[k]);
+        sx[k] = sy[k] = sz[k] = sp[k] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll 4
+    for (int p = 0; p < kTileJ / 2; ++p) {
+        const float4 A = b[2 * p];
+        const float4 B = b[2 * p + 1];
+        const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+        const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const float2 dx = __fadd2_rn(qx, nx[k]);
+            const float2 dy = __fadd2_rn(qy, ny[k]);
+            const float2 dz = __fadd2_rn(qz, nz[k]);
+            float2 r2 = (LAW == NB_LAW_PLUMMER) ? __ffma2_rn(dz, dz, e2[k]) : __fmul2_rn(dz, dz);
+            r2 = __ffma2_rn(dy, dy, r2);
+            r2 = __ffma2_rn(dx, dx, r2);
+            const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+            const float2 mp = __fmul2_rn(qm, rinv);
+            if (ACC) {
+                const float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
+                sx[k] = __ffma2_rn(dx, mr3, sx[k]);
+                sy[k] = __ffma2_rn(dy, mr3, sy[k]);
+                sz[k] = __ffma2_rn(dz, mr3, sz[k]);
+            }
+            if (POT) sp[k] = __fadd2_rn(sp[k], mp);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        ax[k] += sx[k].x + sx[k].y;
+        ay[k] += sy[k].x + sy[k].y;
+        az[k] += sz[k].x + sz[k].y;
+        ap[k] += sp[k].x + sp[k].y;
+    }
+}
+
+template <int LAW, bool ACC, bool POT, int IPT>
+__device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, const float* xr,
+                                                  const float* yr, const float* zr,
+                                                  const float* hh, const float* h2, float* ax,
+                                                  float* ay, float* az, float* ap) {
+#pragma unroll 2
+    for (int p = 0; p < kTileJ / 2; ++p) {
+        const float4 A = b[2 * p];
+        const float4 B = b[2 * p + 1];
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const float4 q = half ? make_float4(A.y, A.w, B.y, B.w) : make_float4(A.x, A.z, B.x, B.z);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float dx = q.x - xr[k];
+                const float dy = q.y - yr[k];
+                const float dz = q.z - zr[k];
+                float r2;
+                if (LAW == NB_LAW_PLUMMER)
+                    r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, h2[k])));
+                else
+                    r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const float rinv = rsqrt_approx(r2);
+                float mp = q.w * rinv;
+                float mr3 = mp * rinv * rinv;
+                if (LAW == NB_LAW_SPLINE_G2) {
+                    if (r2 < h2[k]) spline_close(r2, rinv, q.w, hh[k], mr3, mp);
+                }
+                if (ACC) {
+                    ax[k] = fmaf(dx, mr3, ax[k]);
+                    ay[k] = fmaf(dy, mr3, ay[k]);
+                    az[k] = fmaf(dz, mr3, az[k]);
+                }
+                if (POT) ap[k] += mp;
+            }
+        }
+    }
+}
+
+}  // namespace nb

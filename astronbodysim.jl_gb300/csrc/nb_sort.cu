@@ -220,6 +220,13 @@ __global__ void __launch_bounds__(kSortThreads)
     }
 }
 
+// Exclusive prefix sum of len 32-bit counts in place (one CTA of 1024 threads).
+cudaError_t launch_exclusive_scan(uint32_t* counts, int64_t len, cudaStream_t s) {
+    if (len <= 0) return cudaSuccess;
+    k_scan<<<1, 1024, 0, s>>>(counts, len);
+    return cudaGetLastError();
+}
+
 // Computes perm[0..n) = particle indices in Morton order of (x, y, z).
 cudaError_t launch_morton_sort(const double* x, const double* y, const double* z, int64_t n,
                                void* scratch, int32_t* perm, cudaStream_t s) {

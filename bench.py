@@ -321,7 +321,9 @@ def run_gpu(args):
                        "step": "drift+pack+force(N^2)+kick, one CUDA graph replay",
                        "l2": "256 MiB write between timed steps, outside the events",
                        "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "block": sim.params.block or 128, "i_per_thread": sim.params.i_per_thread or 2},
+                       "force_kernel": ("auto: direct grid 128 threads x 1 target for N >= 2^19, "
+                                        "persistent work list below" if not (args.block or args.ipt)
+                                        else "block=%d i_per_thread=%d" % (args.block, args.ipt))},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak_tflops,
                          "unit": "TFLOP/s", "frac": achieved / fp32_peak_tflops, "traffic": traffic,
                          "kernel": "k_force_mixed (+k_pack)", "force_ms": force_ms,

@@ -66,7 +66,8 @@ typedef struct nb_params {
     int32_t device;       /* CUDA ordinal */
     int32_t tile_j;       /* tuning override: j-tile (0 = auto) */
     int32_t i_per_thread; /* tuning override (0 = auto) */
-    int32_t block;        /* tuning override: threads per CTA (0 = auto) */
+    int32_t block;        /* tuning override: threads per CTA of the direct grid (128, 256);
+                             -1 = persistent work-list kernel; 0 (with i_per_thread 0) = auto */
 } nb_params;
 
 /* Energy / momentum diagnostics, FP64 (src/base/Energy.jl:13-101). */
