@@ -66,6 +66,35 @@ class nb_params(ctypes.Structure):
     ]
 
 
+class nb_engine_params(ctypes.Structure):
+    _fields_ = [
+        ("G", ctypes.c_double),
+        ("law", ctypes.c_int32),
+        ("device", ctypes.c_int32),
+        ("max_particles", ctypes.c_int64),
+        ("max_systems", ctypes.c_int32),
+        ("max_steps_per_call", ctypes.c_int32),
+    ]
+
+
+class nb_engine_stats(ctypes.Structure):
+    _fields_ = [
+        ("queued", ctypes.c_int64),
+        ("running", ctypes.c_int64),
+        ("done", ctypes.c_int64),
+        ("resident_particles", ctypes.c_int64),
+        ("engine_steps", ctypes.c_int64),
+        ("interactions", ctypes.c_double),
+        ("gpu_ms", ctypes.c_double),
+    ]
+
+
+NB_REQ_QUEUED = 0
+NB_REQ_RUNNING = 1
+NB_REQ_DONE = 2
+NB_REQ_CANCELLED = 3
+
+
 class nb_diag(ctypes.Structure):
     _fields_ = [
         ("kinetic", ctypes.c_double),
@@ -111,6 +140,16 @@ SIGNATURES = {
     "nb_force_noalloc": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int32,
                                         ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp,
                                         ctypes.c_char_p, ctypes.c_int64]),
+    "nb_engine_create": (ctypes.c_int, [ctypes.POINTER(nb_engine_params), ctypes.POINTER(_h)]),
+    "nb_engine_destroy": (ctypes.c_int, [_h]),
+    "nb_batch_submit": (ctypes.c_int, [_h, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_int64, _i64p]),
+    "nb_engine_run": (ctypes.c_int, [_h, ctypes.c_int64, _i64p]),
+    "nb_batch_poll": (ctypes.c_int, [_h, ctypes.c_int64, _i32p, _i64p]),
+    "nb_batch_fetch": (ctypes.c_int, [_h, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "nb_batch_cancel": (ctypes.c_int, [_h, ctypes.c_int64]),
+    "nb_engine_get_stats": (ctypes.c_int, [_h, ctypes.POINTER(nb_engine_stats)]),
+    "nb_engine_last_error": (ctypes.c_char_p, [_h]),
     "nb_last_error": (ctypes.c_char_p, [_h]),
     "nb_version": (ctypes.c_char_p, []),
 }

@@ -1,0 +1,488 @@
+// nb_batch.cu -- kernels of the many-system engine (nb_engine.cu).
+//
+// Many independent systems live in one particle arena; system slot s owns a
+// contiguous range of arena particles, and every particle carries its slot
+// (sysid, -1 for free space).  The running systems are ranked 0..R-1; a step
+// of the engine is
+//   drift -> per-system bounding boxes -> Morton keys with the rank in the top
+//   bits -> radix sort (systems stay contiguous, each in its own Z-order) ->
+//   per-system packed FP32 tiles -> force over whole i-blocks -> kick.
+// The force kernel never splits an i-block and a system's sort key depends only
+// on its own particles, so a system's trajectory is bit-identical whether it
+// runs alone or among others.
+#include "nb_pairs.cuh"
+
+namespace nb {
+
+constexpr int kBThreads = 256;
+
+// Per-rank description of a running system (device memory).
+//   aoff: first arena particle, soff: first sorted slot, n: particles.
+__global__ void __launch_bounds__(kBThreads)
+    k_batch_bbox(const BatchSys* __restrict__ bs, const double* __restrict__ x,
+                 const double* __restrict__ y, const double* __restrict__ z,
+                 double* __restrict__ bbox) {
+    __shared__ double red[6][kBThreads / 32];
+    const BatchSys d = bs[blockIdx.x];
+    double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
+    for (int64_t i = threadIdx.x; i < d.n; i += kBThreads) {
+        const int64_t p = d.aoff + i;
+        const double a = x[p], b = y[p], c = z[p];
+        v[0] = fmin(v[0], a);
+        v[1] = fmin(v[1], b);
+        v[2] = fmin(v[2], c);
+        v[3] = fmin(v[3], -a);
+        v[4] = fmin(v[4], -b);
+        v[5] = fmin(v[5], -c);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) red[k][threadIdx.x >> 5] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double r = red[threadIdx.x][0];
+        for (int w = 1; w < kBThreads / 32; ++w) r = fmin(r, red[threadIdx.x][w]);
+        bbox[blockIdx.x * 6 + threadIdx.x] = r;
+    }
+}
+
+// Spreads the low 14 bits of v to every third bit (bits 0, 3, ..., 39).
+__device__ __forceinline__ uint64_t spread3_14(uint64_t v) {
+    v &= 0x3fffull;
+    v = (v | (v << 32)) & 0x1f00000000ffffull;
+    v = (v | (v << 16)) & 0x1f0000ff0000ffull;
+    v = (v | (v << 8)) & 0x100f00f00f00f00full;
+    v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+    v = (v | (v << 2)) & 0x1249249249249249ull;
+    return v;
+}
+
+// key = rank << 42 | Morton code (14 bits per axis over the system's box);
+// free arena space sorts last.
+__global__ void __launch_bounds__(kBThreads)
+    k_batch_keys(const int32_t* __restrict__ sysid, const int32_t* __restrict__ rank_of_slot,
+                 const double* __restrict__ bbox, const double* __restrict__ x,
+                 const double* __restrict__ y, const double* __restrict__ z, int64_t n,
+                 uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
+    if (i >= n) return;
+    const int32_t s = sysid[i];
+    const int32_t r = s >= 0 ? rank_of_slot[s] : -1;
+    uint64_t key = ~0ull;
+    if (r >= 0) {
+        const double* bb = bbox + 6 * (int64_t)r;
+        const double p[3] = {x[i], y[i], z[i]};
+        uint64_t q[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double lo = bb[k], hi = -bb[3 + k];
+            const double ext = hi - lo;
+            double f = ext > 0.0 ? (p[k] - lo) / ext : 0.0;
+            f = fmin(fmax(f, 0.0), 1.0);
+            q[k] = (uint64_t)(f * 16383.0);
+        }
+        key = ((uint64_t)r << 42) | spread3_14(q[0]) | (spread3_14(q[1]) << 1) |
+              (spread3_14(q[2]) << 2);
+    }
+    keys[i] = key;
+    vals[i] = (int32_t)i;
+}
+
+// One CTA per packed tile: tile g belongs to rank tile_rank[g]; same per-tile
+// origin, radius and paired layout as the single-system pack.
+__global__ void __launch_bounds__(kTileJ)
+    k_batch_pack(const int32_t* __restrict__ tile_rank, const SysDesc* __restrict__ sys,
+                 const int32_t* __restrict__ perm, const double* __restrict__ x,
+                 const double* __restrict__ y, const double* __restrict__ z,
+                 const double* __restrict__ m, float4* __restrict__ pack,
+                 dvec4* __restrict__ origin) {
+    __shared__ double red[6][kTileJ / 32];
+    const int32_t g = blockIdx.x;
+    const SysDesc& d = sys[tile_rank[g]];
+    const int32_t t = g - d.tile_off;
+    const int32_t slot = t * kTileJ + threadIdx.x;
+    const bool valid = slot < d.n;
+    double px = 0.0, py = 0.0, pz = 0.0, pm = 0.0;
+    if (valid) {
+        const int32_t p = perm[d.off + slot];
+        px = x[p];
+        py = y[p];
+        pz = z[p];
+        pm = m[p];
+    }
+    double v[6];
+    v[0] = valid ? px : 1e300;
+    v[1] = valid ? py : 1e300;
+    v[2] = valid ? pz : 1e300;
+    v[3] = valid ? -px : 1e300;
+    v[4] = valid ? -py : 1e300;
+    v[5] = valid ? -pz : 1e300;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
+    __syncthreads();
+    double lo[3], hi[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double a = red[k][0], b = red[k + 3][0];
+#pragma unroll
+        for (int w = 1; w < kTileJ / 32; ++w) {
+            a = fmin(a, red[k][w]);
+            b = fmin(b, red[k + 3][w]);
+        }
+        lo[k] = a;
+        hi[k] = -b;
+    }
+    const double ox = 0.5 * (lo[0] + hi[0]);
+    const double oy = 0.5 * (lo[1] + hi[1]);
+    const double oz = 0.5 * (lo[2] + hi[2]);
+    float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
+    if (valid) {
+        qx = (float)(px - ox);
+        qy = (float)(py - oy);
+        qz = (float)(pz - oz);
+        qm = (float)pm;
+    }
+    float* base = reinterpret_cast<float*>(pack + (int64_t)g * kTileJ);
+    const int pr = threadIdx.x >> 1, half = threadIdx.x & 1;
+    base[8 * pr + half] = qx;
+    base[8 * pr + 2 + half] = qy;
+    base[8 * pr + 4 + half] = qz;
+    base[8 * pr + 6 + half] = qm;
+    if (threadIdx.x == 0) {
+        const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+        origin[g] = make_dvec4(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Force over whole i-blocks.  items[k] = (rank, i-block), largest systems
+// first; persistent CTAs claim items from a device counter.  Within an item
+// the CTA streams all j-tiles of that system through the bulk-copy ring, in
+// order, exactly like the single-system kernel.
+// ---------------------------------------------------------------------------
+constexpr int kFBlock = 128;
+constexpr int kFIpt = 2;
+constexpr int kFBt = kFBlock * kFIpt;
+
+template <int LAW, bool ACC, bool POT>
+__global__ void __launch_bounds__(kFBlock, (ACC && !POT) ? 8 : 1) k_force_batch(BatchForce f) {
+    constexpr int IPT = kFIpt;
+    constexpr int BLOCK = kFBlock;
+    constexpr int NW = kFBlock / 32;
+    __shared__ __align__(128) float4 buf[kStages * kTileJ];
+    __shared__ __align__(8) uint64_t full[kStages];
+    __shared__ uint32_t done[kStages];
+    __shared__ int32_t item_sh;
+    __shared__ uint32_t abort_sh;
+    __shared__ double tpx[kFBt], tpy[kFBt], tpz[kFBt];
+    const int tid = threadIdx.x, lane = tid & 31;
+
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 1);
+            done[s] = 0;
+        }
+        abort_sh = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    uint32_t vbase = 0;  // tiles streamed so far by this CTA (ring phase)
+    uint32_t last_issued = 0;
+    for (;;) {
+        if (tid == 0) item_sh = atomicAdd(f.counter, 1);
+        __syncthreads();
+        const int32_t it = item_sh;
+        if (it >= f.nitems || abort_sh) break;  // CTA-uniform
+        const int2 ib = f.items[it];
+        const SysDesc& d = f.sys[ib.x];
+        const int32_t ntiles = d.ntiles;
+        if (tid == 0) {
+            for (int k = 0; k < kStages && k < ntiles; ++k) {
+                const uint32_t v = vbase + k;
+                mbar_arrive_expect_tx(&full[v % kStages], kTileJ * sizeof(float4));
+                bulk_g2s(&buf[(v % kStages) * kTileJ], f.pack + (int64_t)(d.tile_off + k) * kTileJ,
+                         kTileJ * sizeof(float4), &full[v % kStages]);
+                last_issued = v + 1;
+            }
+        }
+        int32_t pidx[IPT];
+        float hh[IPT], h2[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const int32_t slot = ib.y * kFBt + k * BLOCK + tid;
+            pidx[k] = -1;
+            double x = 0.0, y = 0.0, z = 0.0;
+            if (slot < d.n) {
+                const int32_t p = f.perm[d.off + slot];
+                pidx[k] = p;
+                x = f.x[p];
+                y = f.y[p];
+                z = f.z[p];
+            }
+            tpx[k * BLOCK + tid] = x;
+            tpy[k * BLOCK + tid] = y;
+            tpz[k * BLOCK + tid] = z;
+            hh[k] = (float)d.soft[0];
+            h2[k] = hh[k] * hh[k];
+        }
+        float sx[IPT], sy[IPT], sz[IPT], sp[IPT];
+        float cx[IPT], cy[IPT], cz[IPT], cp[IPT];
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            sx[k] = sy[k] = sz[k] = sp[k] = 0.0f;
+            cx[k] = cy[k] = cz[k] = cp[k] = 0.0f;
+        }
+        bool timed_out = false;
+        for (int32_t t = 0; t < ntiles; ++t) {
+            const uint32_t v = vbase + t;
+            const int st = (int)(v % kStages);
+            const uint32_t par = (v / kStages) & 1u;
+            const dvec4 o = f.origin[d.tile_off + t];
+            float xr[IPT], yr[IPT], zr[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                xr[k] = (float)(tpx[k * BLOCK + tid] - o.x);
+                yr[k] = (float)(tpy[k * BLOCK + tid] - o.y);
+                zr[k] = (float)(tpz[k * BLOCK + tid] - o.z);
+            }
+            float ax[IPT], ay[IPT], az[IPT], ap[IPT];
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) ax[k] = ay[k] = az[k] = ap[k] = 0.0f;
+            if (!__all_sync(0xffffffffu, mbar_wait_bounded(&full[st], par, kWaitTimeoutNs))) {
+                timed_out = true;
+                if (lane == 0) {
+                    atomicOr(f.err, DEVERR_TIMEOUT);
+                    atomicExch(&abort_sh, 1u);
+                }
+                break;
+            }
+            const float4* b = &buf[st * kTileJ];
+            bool near = false;
+            if (LAW == NB_LAW_SPLINE_G2) {
+                const float R = (float)o.w;
+#pragma unroll
+                for (int k = 0; k < IPT; ++k) {
+                    const float d2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
+                    const float lim = (R + hh[k]) * 1.0001f;
+                    near |= (pidx[k] >= 0) && (d2 <= lim * lim);
+                }
+                near = __any_sync(0xffffffffu, near);
+            }
+            if (near)
+                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+            else
+                pair_loop_fast<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap);
+            __syncwarp();
+            if (lane == 0) {
+                __threadfence_block();
+                const uint32_t prev = atomicAdd(&done[st], 1u);
+                if (prev == NW - 1) {
+                    __threadfence_block();
+                    done[st] = 0;
+                    if (t + kStages < ntiles) {
+                        mbar_arrive_expect_tx(&full[st], kTileJ * sizeof(float4));
+                        bulk_g2s(&buf[st * kTileJ],
+                                 f.pack + (int64_t)(d.tile_off + t + kStages) * kTileJ,
+                                 kTileJ * sizeof(float4), &full[st]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                if (ACC) {
+                    two_sum_acc(sx[k], cx[k], ax[k]);
+                    two_sum_acc(sy[k], cy[k], ay[k]);
+                    two_sum_acc(sz[k], cz[k], az[k]);
+                }
+                if (POT) two_sum_acc(sp[k], cp[k], ap[k]);
+            }
+        }
+        if (!timed_out) {
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const int32_t p = pidx[k];
+                if (p < 0) continue;
+                if (ACC) {
+                    f.ax[p] = ((double)sx[k] + (double)cx[k]) * f.G;
+                    f.ay[p] = ((double)sy[k] + (double)cy[k]) * f.G;
+                    f.az[p] = ((double)sz[k] + (double)cz[k]) * f.G;
+                }
+                if (POT) {
+                    double phi = -((double)sp[k] + (double)cp[k]);
+                    if (LAW == NB_LAW_PLUMMER) phi += (double)((float)f.m[p] * rsqrt_approx(h2[k]));
+                    f.pot[p] = phi * f.G;
+                }
+            }
+        }
+        vbase += (uint32_t)ntiles;
+        __syncthreads();  // every warp is done with this item's tiles
+    }
+    if (abort_sh && tid == 0) {
+        // Drain the copies that may still be in flight (at most kStages).
+        for (uint32_t u = last_issued > kStages ? last_issued - kStages : 0; u < last_issued; ++u)
+            (void)mbar_wait_bounded(&full[u % kStages], (u / kStages) & 1u, kWaitTimeoutNs / 8);
+    }
+}
+
+template <int LAW, bool ACC, bool POT>
+static int batch_occ() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_batch<LAW, ACC, POT>, kFBlock,
+                                                      0) != cudaSuccess)
+        return 1;
+    return nb < 1 ? 1 : nb;
+}
+
+int batch_ctas_per_sm(int law, bool acc, bool pot) {
+    if (law == NB_LAW_PLUMMER) {
+        if (!acc) return batch_occ<NB_LAW_PLUMMER, false, true>();
+        return pot ? batch_occ<NB_LAW_PLUMMER, true, true>() : batch_occ<NB_LAW_PLUMMER, true, false>();
+    }
+    if (!acc) return batch_occ<NB_LAW_SPLINE_G2, false, true>();
+    return pot ? batch_occ<NB_LAW_SPLINE_G2, true, true>() : batch_occ<NB_LAW_SPLINE_G2, true, false>();
+}
+
+int batch_block_targets() { return kFBt; }
+
+template <int LAW, bool ACC, bool POT>
+static cudaError_t launch_fb(const BatchForce& f, int grid, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(f.counter, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return e;
+    k_force_batch<LAW, ACC, POT><<<grid, kFBlock, 0, s>>>(f);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, cudaStream_t s) {
+    const bool acc = f.ax != nullptr, pot = f.pot != nullptr;
+    if (f.nitems <= 0 || grid <= 0 || (!acc && !pot)) return cudaSuccess;
+    if (law == NB_LAW_PLUMMER) {
+        if (!acc) return launch_fb<NB_LAW_PLUMMER, false, true>(f, grid, s);
+        return pot ? launch_fb<NB_LAW_PLUMMER, true, true>(f, grid, s)
+                   : launch_fb<NB_LAW_PLUMMER, true, false>(f, grid, s);
+    }
+    if (!acc) return launch_fb<NB_LAW_SPLINE_G2, false, true>(f, grid, s);
+    return pot ? launch_fb<NB_LAW_SPLINE_G2, true, true>(f, grid, s)
+               : launch_fb<NB_LAW_SPLINE_G2, true, false>(f, grid, s);
+}
+
+// ---------------------------------------------------------------------------
+// Integrator over the arena (FP64; built with -fmad=false in nb_integrate.cu's
+// spirit: explicit round-to-nearest intrinsics keep each product and sum
+// rounded as the reference's Julia expressions are).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBThreads)
+    k_batch_drift(double* __restrict__ x, double* __restrict__ y, double* __restrict__ z,
+                  const double* __restrict__ vx, const double* __restrict__ vy,
+                  const double* __restrict__ vz, const int32_t* __restrict__ sysid,
+                  const double* __restrict__ dt_slot, const double* __restrict__ fac_slot,
+                  int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
+    if (i >= n) return;
+    const int32_t s = sysid[i];
+    if (s < 0) return;
+    const double f = fac_slot[s];
+    if (f == 0.0) return;
+    const double dt = __dmul_rn(dt_slot[s], f);
+    x[i] = __dadd_rn(x[i], __dmul_rn(vx[i], dt));
+    y[i] = __dadd_rn(y[i], __dmul_rn(vy[i], dt));
+    z[i] = __dadd_rn(z[i], __dmul_rn(vz[i], dt));
+}
+
+// v += a * (dt * fac): fac 1 for a full kick, +-0.5 for the leapfrog half
+// kicks at admission and retirement (src/base/Timestep.jl:84-93, 116-125).
+__global__ void __launch_bounds__(kBThreads)
+    k_batch_kick(double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
+                 const double* __restrict__ ax, const double* __restrict__ ay,
+                 const double* __restrict__ az, const int32_t* __restrict__ sysid,
+                 const double* __restrict__ dt_slot, const double* __restrict__ fac_slot,
+                 int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
+    if (i >= n) return;
+    const int32_t s = sysid[i];
+    if (s < 0) return;
+    const double f = fac_slot[s];
+    if (f == 0.0) return;
+    // Same operation order as the single-system kernels: a * fw * 0.5 * dt for
+    // half kicks, a * dt for full kicks.
+    if (f == 1.0) {
+        const double dt = dt_slot[s];
+        vx[i] = __dadd_rn(vx[i], __dmul_rn(ax[i], dt));
+        vy[i] = __dadd_rn(vy[i], __dmul_rn(ay[i], dt));
+        vz[i] = __dadd_rn(vz[i], __dmul_rn(az[i], dt));
+    } else {
+        const double fw = f > 0.0 ? 1.0 : -1.0;
+        const double dt = dt_slot[s];
+        vx[i] = __dadd_rn(vx[i], __dmul_rn(__dmul_rn(__dmul_rn(ax[i], fw), 0.5), dt));
+        vy[i] = __dadd_rn(vy[i], __dmul_rn(__dmul_rn(__dmul_rn(ay[i], fw), 0.5), dt));
+        vz[i] = __dadd_rn(vz[i], __dmul_rn(__dmul_rn(__dmul_rn(az[i], fw), 0.5), dt));
+    }
+}
+
+__global__ void k_fill_i32(int32_t* __restrict__ a, int64_t n, int32_t v) {
+    const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
+    if (i < n) a[i] = v;
+}
+
+cudaError_t launch_fill_i32(int32_t* a, int64_t n, int32_t v, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_fill_i32<<<(unsigned)((n + kBThreads - 1) / kBThreads), kBThreads, 0, s>>>(a, n, v);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_bbox(const BatchSys* bs, int32_t nrank, const double* x, const double* y,
+                              const double* z, double* bbox, cudaStream_t s) {
+    if (nrank <= 0) return cudaSuccess;
+    k_batch_bbox<<<nrank, kBThreads, 0, s>>>(bs, x, y, z, bbox);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot, const double* bbox,
+                              const double* x, const double* y, const double* z, int64_t n,
+                              uint64_t* keys, int32_t* vals, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_batch_keys<<<(unsigned)((n + kBThreads - 1) / kBThreads), kBThreads, 0, s>>>(
+        sysid, rank_of_slot, bbox, x, y, z, n, keys, vals);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
+                              const int32_t* perm, const double* x, const double* y,
+                              const double* z, const double* m, float4* pack, dvec4* origin,
+                              cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, perm, x, y, z, m, pack, origin);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_drift(double* x, double* y, double* z, const double* vx, const double* vy,
+                               const double* vz, const int32_t* sysid, const double* dt_slot,
+                               const double* fac_slot, int64_t n, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_batch_drift<<<(unsigned)((n + kBThreads - 1) / kBThreads), kBThreads, 0, s>>>(
+        x, y, z, vx, vy, vz, sysid, dt_slot, fac_slot, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_kick(double* vx, double* vy, double* vz, const double* ax,
+                              const double* ay, const double* az, const int32_t* sysid,
+                              const double* dt_slot, const double* fac_slot, int64_t n,
+                              cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_batch_kick<<<(unsigned)((n + kBThreads - 1) / kBThreads), kBThreads, 0, s>>>(
+        vx, vy, vz, ax, ay, az, sysid, dt_slot, fac_slot, n);
+    return cudaGetLastError();
+}
+
+}  // namespace nb

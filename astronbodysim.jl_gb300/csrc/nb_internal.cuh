@@ -135,6 +135,56 @@ int worklist_ctas_per_sm(int law, bool acc, bool pot);
 size_t worklist_partial_bytes(int64_t grid);
 int worklist_block_targets();
 
+// Many-system engine (nb_batch.cu, nb_engine.cu).
+struct BatchSys {
+    int64_t aoff;  // first arena particle
+    int64_t soff;  // first sorted slot
+    int32_t n;
+    int32_t slot;
+};
+
+struct BatchForce {
+    const SysDesc* sys;   // by rank; off = first sorted slot
+    const int2* items;    // (rank, i-block), largest systems first
+    int32_t nitems;
+    int32_t pad;
+    int32_t* counter;     // claim counter, zeroed by the launch
+    const int32_t* perm;  // sorted slot -> arena particle
+    const float4* pack;
+    const dvec4* origin;
+    const double* x;
+    const double* y;
+    const double* z;
+    const double* m;
+    double* ax;
+    double* ay;
+    double* az;
+    double* pot;
+    double G;
+    uint32_t* err;
+};
+
+cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, cudaStream_t s);
+cudaError_t launch_fill_i32(int32_t* a, int64_t n, int32_t v, cudaStream_t s);
+int batch_ctas_per_sm(int law, bool acc, bool pot);
+int batch_block_targets();
+cudaError_t launch_batch_bbox(const BatchSys* bs, int32_t nrank, const double* x, const double* y,
+                              const double* z, double* bbox, cudaStream_t s);
+cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot, const double* bbox,
+                              const double* x, const double* y, const double* z, int64_t n,
+                              uint64_t* keys, int32_t* vals, cudaStream_t s);
+cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
+                              const int32_t* perm, const double* x, const double* y,
+                              const double* z, const double* m, float4* pack, dvec4* origin,
+                              cudaStream_t s);
+cudaError_t launch_batch_drift(double* x, double* y, double* z, const double* vx, const double* vy,
+                               const double* vz, const int32_t* sysid, const double* dt_slot,
+                               const double* fac_slot, int64_t n, cudaStream_t s);
+cudaError_t launch_batch_kick(double* vx, double* vy, double* vz, const double* ax,
+                              const double* ay, const double* az, const int32_t* sysid,
+                              const double* dt_slot, const double* fac_slot, int64_t n,
+                              cudaStream_t s);
+
 // Launch helpers implemented in the .cu files.
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
                         int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
@@ -144,6 +194,8 @@ cudaError_t launch_pack(const double* x, const double* y, const double* z, const
 size_t sort_scratch_bytes(int64_t n);
 cudaError_t launch_morton_sort(const double* x, const double* y, const double* z, int64_t n,
                                void* scratch, int32_t* perm, cudaStream_t s);
+uint64_t* sort_keys_buffer(void* scratch, int64_t n);
+cudaError_t launch_sort_keys(void* scratch, int64_t n, int32_t* vals, int passes, cudaStream_t s);
 cudaError_t launch_force_mixed(int law, bool pot, const Sources32& src, const Targets& tg,
                                double G, uint32_t* err, int block, int ipt, cudaStream_t s);
 cudaError_t launch_force_fp64(int law, bool pot, const Sources64& src, const Targets& tg,

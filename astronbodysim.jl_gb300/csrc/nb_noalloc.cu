@@ -46,7 +46,8 @@ constexpr size_t kOffSort = kOffErr + 256;
 constexpr size_t kSortBytes = 2 * al256(8 * kNoAllocMaxParticles) +
                               al256(4 * kNoAllocMaxParticles) +
                               al256(4 * 256 * ((kNoAllocMaxParticles + 2047) / 2048)) +
-                              al256(8 * 6 * 256) + al256(8 * 8);
+                              al256(8 * 6 * 256) + al256(8 * 8) +
+                              al256(4 * ((256 * ((kNoAllocMaxParticles + 2047) / 2048) + 4095) / 4096 + 1));
 constexpr size_t kScratchBytes = kOffSort + kSortBytes;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];

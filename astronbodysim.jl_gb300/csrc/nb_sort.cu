@@ -24,6 +24,8 @@ constexpr int kWarps = kSortThreads / 32;
 constexpr int kBboxBlocks = 256;
 
 int64_t sort_blocks(int64_t n) { return (n + kSortTile - 1) / kSortTile; }
+int64_t scan_tmp_words(int64_t len);
+cudaError_t launch_exclusive_scan2(uint32_t* counts, int64_t len, uint32_t* tmp, cudaStream_t s);
 
 // Scratch layout (bytes) for n particles.
 size_t sort_scratch_bytes(int64_t n) {
@@ -31,7 +33,7 @@ size_t sort_scratch_bytes(int64_t n) {
     auto al = [](size_t v) { return (v + 255) / 256 * 256; };
     return al(sizeof(uint64_t) * n) * 2 + al(sizeof(int32_t) * n) +
            al(sizeof(uint32_t) * (size_t)kRadix * nb) + al(sizeof(double) * 6 * kBboxBlocks) +
-           al(sizeof(double) * 8);
+           al(sizeof(double) * 8) + al(sizeof(uint32_t) * (size_t)scan_tmp_words(kRadix * nb));
 }
 
 struct SortScratch {
@@ -41,6 +43,7 @@ struct SortScratch {
     uint32_t* counts;
     double* bbox_part;
     double* bbox;
+    uint32_t* scan_tmp;
 };
 
 static SortScratch carve(void* base, int64_t n) {
@@ -58,6 +61,8 @@ static SortScratch carve(void* base, int64_t n) {
     s.bbox_part = (double*)p;
     p += al(sizeof(double) * 6 * kBboxBlocks);
     s.bbox = (double*)p;
+    p += al(sizeof(double) * 8);
+    s.scan_tmp = (uint32_t*)p;
     return s;
 }
 
@@ -220,10 +225,116 @@ __global__ void __launch_bounds__(kSortThreads)
     }
 }
 
+// Multi-CTA exclusive scan for long arrays: each CTA sums a chunk of
+// kScanChunk counts, one CTA scans the chunk sums, each CTA rescans its chunk
+// from its offset.
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 16;
+constexpr int kScanChunk = kScanThreads * kScanPer;
+constexpr int64_t kScanMaxChunks = 1024;  // chunk sums scanned by one k_scan CTA
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_chunk_sums(const uint32_t* __restrict__ c, int64_t len, uint32_t* __restrict__ sums) {
+    const int64_t b = (int64_t)blockIdx.x * kScanChunk;
+    uint32_t s = 0;
+    for (int i = threadIdx.x; i < kScanChunk; i += kScanThreads) {
+        const int64_t j = b + i;
+        if (j < len) s += c[j];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ uint32_t w[kScanThreads / 32];
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int k = 0; k < kScanThreads / 32; ++k) t += w[k];
+        sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_chunk_apply(uint32_t* __restrict__ c, int64_t len, const uint32_t* __restrict__ offs) {
+    __shared__ uint32_t part[kScanThreads];
+    const int64_t b = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanPer;
+    uint32_t v[kScanPer];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        const int64_t j = b + k;
+        v[k] = j < len ? c[j] : 0u;
+        s += v[k];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < kScanThreads; o <<= 1) {
+        const uint32_t t = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += t;
+        __syncthreads();
+    }
+    uint32_t run = offs[blockIdx.x] + part[threadIdx.x] - s;
+#pragma unroll
+    for (int k = 0; k < kScanPer; ++k) {
+        const int64_t j = b + k;
+        if (j < len) c[j] = run;
+        run += v[k];
+    }
+}
+
+// Exclusive prefix sum of len 32-bit counts in place.  `tmp` (may be null for
+// len <= kScanChunk * 4) holds scan_tmp_words(len) words.
+int64_t scan_tmp_words(int64_t len) { return (len + kScanChunk - 1) / kScanChunk + 1; }
+
+cudaError_t launch_exclusive_scan2(uint32_t* counts, int64_t len, uint32_t* tmp, cudaStream_t s) {
+    if (len <= 0) return cudaSuccess;
+    const int64_t nchunks = (len + kScanChunk - 1) / kScanChunk;
+    if (!tmp || nchunks <= 4 || nchunks > kScanMaxChunks * kScanChunk) {
+        k_scan<<<1, 1024, 0, s>>>(counts, len);
+        return cudaGetLastError();
+    }
+    k_scan_chunk_sums<<<(unsigned)nchunks, kScanThreads, 0, s>>>(counts, len, tmp);
+    k_scan<<<1, 1024, 0, s>>>(tmp, nchunks);
+    k_scan_chunk_apply<<<(unsigned)nchunks, kScanThreads, 0, s>>>(counts, len, tmp);
+    return cudaGetLastError();
+}
+
 // Exclusive prefix sum of len 32-bit counts in place (one CTA of 1024 threads).
 cudaError_t launch_exclusive_scan(uint32_t* counts, int64_t len, cudaStream_t s) {
     if (len <= 0) return cudaSuccess;
     k_scan<<<1, 1024, 0, s>>>(counts, len);
+    return cudaGetLastError();
+}
+
+// Key buffer inside a sort scratch of sort_scratch_bytes(n) bytes.
+uint64_t* sort_keys_buffer(void* scratch, int64_t n) { return carve(scratch, n).keys_a; }
+
+// Stable LSD radix sort of (keys, vals): keys in sort_keys_buffer(scratch, n),
+// vals (n int32) in place; `passes` 8-bit digits from the bottom (even).
+cudaError_t launch_sort_keys(void* scratch, int64_t n, int32_t* vals, int passes, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    SortScratch sc = carve(scratch, n);
+    const int nblocks = (int)sort_blocks(n);
+    cudaError_t e = cudaSuccess;
+    uint64_t* kin = sc.keys_a;
+    uint64_t* kout = sc.keys_b;
+    int32_t* vin = vals;
+    int32_t* vout = sc.vals_b;
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = pass * kRadixBits;
+        k_radix_hist<<<nblocks, kSortThreads, 0, s>>>(kin, n, shift, nblocks, sc.counts);
+        e = launch_exclusive_scan2(sc.counts, (int64_t)kRadix * nblocks, sc.scan_tmp, s);
+        if (e != cudaSuccess) return e;
+        k_radix_scatter<<<nblocks, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, nblocks,
+                                                         sc.counts);
+        uint64_t* tk = kin;
+        kin = kout;
+        kout = tk;
+        int32_t* tv = vin;
+        vin = vout;
+        vout = tv;
+    }
+    // After an even number of passes the sorted values are back in vals.
     return cudaGetLastError();
 }
 
@@ -236,28 +347,8 @@ cudaError_t launch_morton_sort(const double* x, const double* y, const double* z
     const int bb = (int)(gb < kBboxBlocks ? gb : kBboxBlocks);
     k_bbox_partial<<<bb, kSortThreads, 0, s>>>(x, y, z, n, sc.bbox_part);
     k_bbox_final<<<1, 32, 0, s>>>(sc.bbox_part, bb, sc.bbox);
-    // keys_a / perm hold (key, index); passes alternate between (a, perm) and (b, vals_b)
     k_morton<<<(unsigned)gb, kSortThreads, 0, s>>>(x, y, z, n, sc.bbox, sc.keys_a, perm);
-    const int nblocks = (int)sort_blocks(n);
-    uint64_t* kin = sc.keys_a;
-    uint64_t* kout = sc.keys_b;
-    int32_t* vin = perm;
-    int32_t* vout = sc.vals_b;
-    for (int pass = 0; pass < 8; ++pass) {
-        const int shift = pass * kRadixBits;
-        k_radix_hist<<<nblocks, kSortThreads, 0, s>>>(kin, n, shift, nblocks, sc.counts);
-        k_scan<<<1, 1024, 0, s>>>(sc.counts, (int64_t)kRadix * nblocks);
-        k_radix_scatter<<<nblocks, kSortThreads, 0, s>>>(kin, vin, kout, vout, n, shift, nblocks,
-                                                         sc.counts);
-        uint64_t* tk = kin;
-        kin = kout;
-        kout = tk;
-        int32_t* tv = vin;
-        vin = vout;
-        vout = tv;
-    }
-    // After an even number of passes the sorted values are back in perm.
-    return cudaGetLastError();
+    return launch_sort_keys(scratch, n, perm, 8, s);
 }
 
 }  // namespace nb

@@ -196,6 +196,62 @@ int nb_force_noalloc(int64_t n, const double *x, const double *y, const double *
                      double *ay, double *az, double *pot, void *stream, char *errbuf,
                      int64_t errbuf_len);
 
+/* ---- many-system engine (batching and serving) -------------------------
+ * No single counterpart in the reference: AstroNbodySim.jl runs one
+ * Simulation at a time.  The engine keeps many independent systems resident in
+ * one particle arena, advances all of them together with the same kernels as
+ * step(sim, DirectSum, GPU) (constant-step leapfrog, mixed precision), and
+ * admits queued systems as arena space and slots free up (continuous
+ * batching).  Each system is integrated exactly as run(sim) does
+ * (src/run.jl:76-87, 101-173): force, +1/2 kick, nsteps x (drift, force,
+ * kick), -1/2 kick.  A system's result does not depend on the other systems in
+ * the mix (bit-identical alone or together). */
+typedef struct nb_engine nb_engine;
+
+typedef struct nb_engine_params {
+    double G;
+    int32_t law;                /* NB_LAW_* for every system */
+    int32_t device;
+    int64_t max_particles;      /* arena capacity: the footprint budget of admission */
+    int32_t max_systems;        /* resident system slots */
+    int32_t max_steps_per_call; /* steps between admission rounds in nb_engine_run (0 = 64) */
+} nb_engine_params;
+
+#define NB_REQ_QUEUED 0
+#define NB_REQ_RUNNING 1
+#define NB_REQ_DONE 2
+#define NB_REQ_CANCELLED 3
+
+typedef struct nb_engine_stats {
+    int64_t queued;
+    int64_t running;
+    int64_t done;
+    int64_t resident_particles;
+    int64_t engine_steps;       /* engine steps executed (all resident systems advance) */
+    double interactions;        /* sum over steps and systems of n^2 */
+    double gpu_ms;              /* CUDA-event time of the engine steps */
+} nb_engine_stats;
+
+int nb_engine_create(const nb_engine_params *p, nb_engine **out);
+int nb_engine_destroy(nb_engine *e);
+/* Queue one system (host SoA arrays, copied): n particles, Plummer/spline
+ * softening, constant dt, nsteps KDK steps.  Returns its id.  A system larger
+ * than the whole arena or than a slot allows is rejected with NB_ERR_ADMISSION. */
+int nb_batch_submit(nb_engine *e, int64_t n, const double *x, const double *y, const double *z,
+                    const double *vx, const double *vy, const double *vz, const double *m,
+                    double softening, double dt, int64_t nsteps, int64_t *id);
+/* Admit what fits, then advance every resident system by up to max_steps steps
+ * (fewer when a system finishes earlier or max_steps_per_call is reached);
+ * finished systems are retired and their results kept for nb_batch_fetch. */
+int nb_engine_run(nb_engine *e, int64_t max_steps, int64_t *steps_done);
+int nb_batch_poll(nb_engine *e, int64_t id, int32_t *state, int64_t *steps_done);
+/* Copy the final positions and velocities of a finished system (then forget it). */
+int nb_batch_fetch(nb_engine *e, int64_t id, double *x, double *y, double *z, double *vx,
+                   double *vy, double *vz);
+int nb_batch_cancel(nb_engine *e, int64_t id);
+int nb_engine_get_stats(nb_engine *e, nb_engine_stats *out);
+const char *nb_engine_last_error(nb_engine *e);
+
 /* Last error message of this handle (never NULL). */
 const char *nb_last_error(nb_handle *h);
 

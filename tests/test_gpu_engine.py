@@ -1,0 +1,112 @@
+"""GPU tests of the many-system engine (batching / continuous-batching serving)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def systems(nb, sizes, seed=0):
+    out = []
+    for k, n in enumerate(sizes):
+        d = nb.plummer(n, seed=seed + k) if k % 2 == 0 else nb.hernquist(n, seed=seed + k)
+        out.append(d)
+    return out
+
+
+def test_engine_matches_single_system_path(nb):
+    """Each system of a batch follows the single-system run(sim) trajectory.
+    Both are mixed precision but group sources into different tiles (14- vs
+    21-bit Morton keys), so forces differ at the FP32 level (~1e-7 relative);
+    over 20 steps positions agree to 1e-8 and velocities to 1e-6."""
+    sizes = [300, 1000, 3000, 257]
+    softs = [0.01, 0.005, 0.002, 0.02]
+    dt, nsteps = 1e-3, 20
+    ds = systems(nb, sizes, seed=3)
+    eng = nb.Engine(max_particles=1 << 16, max_systems=64)
+    ids = [eng.submit(d, s, dt, nsteps) for d, s in zip(ds, softs)]
+    eng.run_until_idle()
+    for d, s, rid, n in zip(ds, softs, ids, sizes):
+        assert eng.poll(rid)[0] == nb._lib.NB_REQ_DONE
+        got = eng.fetch(rid, n)
+        sim = nb.Simulation(d, ForceSofteningTable=[s] * 6, TimeStep=dt, TimeEnd=1.0, precision="mixed")
+        nb.run(sim, nsteps=nsteps)
+        ref = nb.get_all_data(sim)
+        np.testing.assert_allclose(got["pos"], ref["pos"], rtol=0, atol=1e-8)
+        np.testing.assert_allclose(got["vel"], ref["vel"], rtol=0, atol=1e-6)
+    st = eng.stats()
+    assert st["done"] == len(sizes) and st["running"] == 0 and st["queued"] == 0
+    assert st["interactions"] == pytest.approx(nsteps * sum(n * n for n in sizes))
+
+
+def test_engine_vs_oracle(nb, oracle):
+    d = nb.plummer(1500, seed=41)
+    h, dt, nsteps = 0.01, 1e-3, 25
+    eng = nb.Engine(max_particles=1 << 14, max_systems=8)
+    rid = eng.submit(d, h, dt, nsteps)
+    eng.run_until_idle()
+    got = eng.fetch(rid, 1500)
+    o = oracle.OracleSim(d["pos"], d["vel"], d["mass"], soft=[h] * 6, dt=dt, time_end=1.0)
+    o.run_begin()
+    o.step(nsteps)
+    o.run_end()
+    np.testing.assert_allclose(got["pos"], o.pos, rtol=0, atol=1e-7)
+    np.testing.assert_allclose(got["vel"], o.vel, rtol=0, atol=1e-5)
+
+
+def test_same_alone_and_in_the_mix(nb):
+    """A system's result does not depend on the other systems (bit-identical):
+    whole i-blocks per work item, per-system Morton keys."""
+    target = nb.plummer(2000, seed=7)
+    others = systems(nb, [512, 4096, 1000, 3333], seed=11)
+    dt, h = 1e-3, 0.004
+    alone = nb.Engine(max_particles=1 << 15, max_systems=16)
+    ra = alone.submit(target, h, dt, 40)
+    alone.run_until_idle()
+    a = alone.fetch(ra, 2000)
+    mix = nb.Engine(max_particles=1 << 15, max_systems=16, max_steps_per_call=7)
+    r0 = mix.submit(others[0], 0.01, dt, 13)       # retires during the target's run
+    r1 = mix.submit(others[1], 0.002, dt, 60)
+    mix.run(5)                                      # others already running
+    rt = mix.submit(target, h, dt, 40)
+    mix.run(9)
+    r2 = mix.submit(others[2], 0.006, dt, 25)       # admitted mid-run
+    r3 = mix.submit(others[3], 0.003, dt, 3)
+    mix.run_until_idle()
+    b = mix.fetch(rt, 2000)
+    np.testing.assert_array_equal(a["pos"], b["pos"])
+    np.testing.assert_array_equal(a["vel"], b["vel"])
+    for rid in (r0, r1, r2, r3):
+        assert mix.poll(rid)[0] == nb._lib.NB_REQ_DONE
+
+
+def test_admission_by_footprint(nb):
+    """Only systems that fit the arena are resident; the rest queue (FIFO)."""
+    ds = systems(nb, [3000, 3000, 3000], seed=21)
+    eng = nb.Engine(max_particles=5000, max_systems=8, max_steps_per_call=4)
+    ids = [eng.submit(d, 0.01, 1e-3, 8) for d in ds]
+    eng.run(1)
+    st = eng.stats()
+    assert st["running"] == 1 and st["queued"] == 2 and st["resident_particles"] == 3000
+    states = [eng.poll(r)[0] for r in ids]
+    assert states == [nb._lib.NB_REQ_RUNNING, nb._lib.NB_REQ_QUEUED, nb._lib.NB_REQ_QUEUED]
+    eng.run_until_idle()
+    assert all(eng.poll(r)[0] == nb._lib.NB_REQ_DONE for r in ids)
+
+
+def test_engine_errors_and_cancel(nb):
+    eng = nb.Engine(max_particles=4096, max_systems=4)
+    big = nb.plummer(5000, seed=1)
+    with pytest.raises(nb.NbodyError) as ei:
+        eng.submit(big, 0.01, 1e-3, 10)
+    assert ei.value.code == nb._lib.NB_ERR_ADMISSION
+    d = nb.plummer(1000, seed=2)
+    r1 = eng.submit(d, 0.01, 1e-3, 10)
+    r2 = eng.submit(d, 0.01, 1e-3, 10)
+    eng.cancel(r2)
+    assert eng.poll(r2)[0] == nb._lib.NB_REQ_CANCELLED
+    with pytest.raises(nb.NbodyError):
+        eng.fetch(r1, 1000)  # not finished
+    eng.run_until_idle()
+    assert eng.poll(r1)[0] == nb._lib.NB_REQ_DONE
+    with pytest.raises(nb.NbodyError):
+        eng.poll(999999)
