@@ -6,6 +6,7 @@ reference's Simulation/run API plus seeded initial conditions.
 """
 from ._lib import NbodyError, load
 from .engine import Engine
+from .serve import RequestStream, ensemble_systems, serve
 from .ics import collision, hernquist, plummer
 from .sim import (DirectSum, GPU, Simulation, active_count, advance_and_find_timestep,
                   compute_force, compute_potential, const_step_count, diagnostics,
@@ -16,7 +17,7 @@ from .sim import (DirectSum, GPU, Simulation, active_count, advance_and_find_tim
                   total_potential)
 
 __all__ = [
-    "Engine", "NbodyError", "load", "plummer", "hernquist", "collision", "DirectSum", "GPU", "Simulation",
+    "Engine", "RequestStream", "ensemble_systems", "serve", "NbodyError", "load", "plummer", "hernquist", "collision", "DirectSum", "GPU", "Simulation",
     "active_count", "advance_and_find_timestep", "compute_force", "compute_potential",
     "const_step_count", "diagnostics", "drift_particles_adaptive_timestep",
     "drift_particles_const_timestep", "find_min_endstep", "force_and_potential_at_points",

@@ -149,6 +149,7 @@ SIGNATURES = {
     "nb_batch_fetch": (ctypes.c_int, [_h, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]),
     "nb_batch_cancel": (ctypes.c_int, [_h, ctypes.c_int64]),
     "nb_engine_get_stats": (ctypes.c_int, [_h, ctypes.POINTER(nb_engine_stats)]),
+    "nb_engine_drain_done": (ctypes.c_int, [_h, _i64p, ctypes.c_int64, _i64p]),
     "nb_engine_last_error": (ctypes.c_char_p, [_h]),
     "nb_last_error": (ctypes.c_char_p, [_h]),
     "nb_version": (ctypes.c_char_p, []),

@@ -91,6 +91,17 @@ class Engine:
     def cancel(self, rid):
         self._ck(self._lib.nb_batch_cancel(self.handle, int(rid)))
 
+    def drain_done(self, cap=4096):
+        """Ids of systems finished since the previous call."""
+        out = []
+        buf = (ctypes.c_int64 * cap)()
+        while True:
+            k = ctypes.c_int64()
+            self._ck(self._lib.nb_engine_drain_done(self.handle, buf, cap, ctypes.byref(k)))
+            out.extend(buf[i] for i in range(k.value))
+            if k.value < cap:
+                return out
+
     def stats(self):
         s = L.nb_engine_stats()
         self._ck(self._lib.nb_engine_get_stats(self.handle, ctypes.byref(s)))

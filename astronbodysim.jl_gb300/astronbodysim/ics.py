@@ -58,6 +58,29 @@ def _hernquist_df(E, G, M, a):
     return M / (8.0 * np.sqrt(2.0) * np.pi ** 3 * a ** 3 * vg ** 3) * num / (1.0 - q2) ** 2.5
 
 
+_ENV_CACHE = {}
+
+
+def _hernquist_envelope_table(G, M, a):
+    """max over v of v^2 f(Phi + v^2/2) tabulated against psi = -Phi a / (G M)
+    in (0, 1); depends only on the model's units, so it is computed once."""
+    key = (G, M, a)
+    if key not in _ENV_CACHE:
+        # dense towards psi -> 0 (outskirts) and psi -> 1 (centre, where f(E)
+        # diverges); the table stops 1e-9 short of the singular point
+        psi = np.unique(np.concatenate([np.geomspace(1e-7, 0.5, 500),
+                                        1.0 - np.geomspace(1e-9, 0.5, 500)]))
+        phi = -psi * G * M / a
+        vesc = np.sqrt(-2.0 * phi)
+        grid = np.linspace(0.0, 1.0, 2049)[1:-1]
+        pmax = np.empty(psi.size)
+        for k in range(0, psi.size, 100):
+            v = vesc[k:k + 100, None] * grid[None, :]
+            pmax[k:k + 100] = (v * v * _hernquist_df(phi[k:k + 100, None] + 0.5 * v * v, G, M, a)).max(1)
+        _ENV_CACHE[key] = (psi, np.log(pmax))
+    return _ENV_CACHE[key]
+
+
 def hernquist(n, seed=0, G=1.0, M=1.0, a=1.0, rmax=100.0, com=True):
     rng = np.random.default_rng(seed)
     umax = (rmax / (rmax + a)) ** 2
@@ -66,14 +89,9 @@ def hernquist(n, seed=0, G=1.0, M=1.0, a=1.0, rmax=100.0, com=True):
     pos = r[:, None] * _isotropic(rng, n)
     phi = -G * M / (r + a)
     vesc = np.sqrt(-2.0 * phi)
-    # envelope of p(v) = v^2 f(phi + v^2/2) from a grid, with margin
-    grid = np.linspace(0.0, 1.0, 129)[1:-1]
-    env = np.zeros(n)
-    for chunk in range(0, n, 1 << 16):
-        sl = slice(chunk, min(n, chunk + (1 << 16)))
-        v = vesc[sl, None] * grid[None, :]
-        p = v * v * _hernquist_df(phi[sl, None] + 0.5 * v * v, G, M, a)
-        env[sl] = 1.3 * p.max(axis=1)
+    # rejection envelope: tabulated maximum of p(v) = v^2 f(phi + v^2/2), with margin
+    psi_t, logp_t = _hernquist_envelope_table(G, M, a)
+    env = 1.3 * np.exp(np.interp(-phi * a / (G * M), psi_t, logp_t))
     speed = np.empty(n)
     todo = np.arange(n)
     while todo.size:

@@ -92,59 +92,214 @@ __global__ void __launch_bounds__(kBThreads)
     vals[i] = (int32_t)i;
 }
 
+// Systems of at most kSmallSort particles are ordered by one CTA each, in
+// shared memory: FP64 bounding box, 14-bit-per-axis Morton code, bitonic sort
+// of (code << 14 | local index), written to perm[soff .. soff + n).  Keys are
+// unique, so the order depends only on the system's own positions.
+constexpr int kSmallSort = 16384;
+constexpr int kSortCta = 1024;
+
+__global__ void __launch_bounds__(kSortCta)
+    k_batch_sort_small(const BatchSys* __restrict__ bs, const int64_t* __restrict__ steps_slot,
+                       int32_t every, int32_t force_all, const double* __restrict__ x,
+                       const double* __restrict__ y, const double* __restrict__ z,
+                       double* __restrict__ bbox, int32_t* __restrict__ lperm) {
+    extern __shared__ uint64_t sk[];
+    __shared__ double red[6][kSortCta / 32];
+    const BatchSys d = bs[blockIdx.x];
+    if (d.n > kSmallSort) return;  // ordered by the global radix sort
+    // Re-ordered at admission and every `every` of the system's own steps, so
+    // the schedule does not depend on the other systems.
+    if (!force_all && steps_slot[d.slot] % every != 0) return;
+    const int tid = threadIdx.x;
+    double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
+    for (int i = tid; i < d.n; i += kSortCta) {
+        const int64_t p = d.aoff + i;
+        const double a = x[p], b = y[p], c = z[p];
+        v[0] = fmin(v[0], a);
+        v[1] = fmin(v[1], b);
+        v[2] = fmin(v[2], c);
+        v[3] = fmin(v[3], -a);
+        v[4] = fmin(v[4], -b);
+        v[5] = fmin(v[5], -c);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    if ((tid & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) red[k][tid >> 5] = v[k];
+    __syncthreads();
+    double lo[3], inv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double a = red[k][0], b = red[k + 3][0];
+        for (int w = 1; w < kSortCta / 32; ++w) {
+            a = fmin(a, red[k][w]);
+            b = fmin(b, red[k + 3][w]);
+        }
+        lo[k] = a;
+        const double ext = -b - a;
+        inv[k] = ext > 0.0 ? 16383.0 / ext : 0.0;
+    }
+    (void)bbox;
+    int np2 = 1;
+    while (np2 < d.n) np2 <<= 1;
+    for (int i = tid; i < np2; i += kSortCta) {
+        uint64_t key = ~0ull;
+        if (i < d.n) {
+            const int64_t p = d.aoff + i;
+            const double q[3] = {x[p], y[p], z[p]};
+            uint64_t c[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double f = (q[k] - lo[k]) * inv[k];
+                f = fmin(fmax(f, 0.0), 16383.0);
+                c[k] = (uint64_t)f;
+            }
+            key = ((spread3_14(c[0]) | (spread3_14(c[1]) << 1) | (spread3_14(c[2]) << 2)) << 14) |
+                  (uint64_t)i;
+        }
+        sk[i] = key;
+    }
+    __syncthreads();
+    for (int k = 2; k <= np2; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < np2; i += kSortCta) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const uint64_t a = sk[i], b = sk[ixj];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        sk[i] = b;
+                        sk[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < d.n; i += kSortCta) lperm[d.aoff + i] = (int32_t)(sk[i] & 0x3fffull);
+}
+
+// Global radix-sort result of the systems too large for shared memory, as
+// arena-relative local order: lperm[aoff + k] = perm[soff + k] - aoff.
+__global__ void __launch_bounds__(kBThreads)
+    k_batch_perm_to_local(const BatchSys* __restrict__ bs, const int32_t* __restrict__ perm,
+                          int32_t* __restrict__ lperm) {
+    const BatchSys d = bs[blockIdx.x];
+    if (d.n <= kSmallSort) return;
+    for (int64_t k = threadIdx.x; k < d.n; k += kBThreads)
+        lperm[d.aoff + k] = (int32_t)(perm[d.soff + k] - d.aoff);
+}
+
+// Per-system step counter (drives the re-ordering schedule).
+__global__ void k_batch_tick(const BatchSys* __restrict__ bs, int32_t nrank,
+                             int64_t* __restrict__ steps_slot) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < nrank) steps_slot[bs[r].slot] += 1;
+}
+
+int batch_small_sort_limit() { return kSmallSort; }
+
+cudaError_t prepare_batch_sort_small() {
+    return cudaFuncSetAttribute(k_batch_sort_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(sizeof(uint64_t) * kSmallSort));
+}
+
+cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t max_small_n,
+                                    const int64_t* steps_slot, int32_t every, int32_t force_all,
+                                    const double* x, const double* y, const double* z,
+                                    double* bbox, int32_t* lperm, cudaStream_t s) {
+    if (nrank <= 0 || max_small_n <= 0) return cudaSuccess;
+    int np2 = 1;
+    while (np2 < max_small_n) np2 <<= 1;
+    k_batch_sort_small<<<nrank, kSortCta, sizeof(uint64_t) * np2, s>>>(bs, steps_slot, every, force_all,
+                                                                        x, y, z, bbox, lperm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_perm_to_local(const BatchSys* bs, int32_t nrank, const int32_t* perm,
+                                       int32_t* lperm, cudaStream_t s) {
+    if (nrank <= 0) return cudaSuccess;
+    k_batch_perm_to_local<<<nrank, kBThreads, 0, s>>>(bs, perm, lperm);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_tick(const BatchSys* bs, int32_t nrank, int64_t* steps_slot, cudaStream_t s) {
+    if (nrank <= 0) return cudaSuccess;
+    k_batch_tick<<<(nrank + 255) / 256, 256, 0, s>>>(bs, nrank, steps_slot);
+    return cudaGetLastError();
+}
+
 // One CTA per packed tile: tile g belongs to rank tile_rank[g]; same per-tile
 // origin, radius and paired layout as the single-system pack.
 __global__ void __launch_bounds__(kTileJ)
     k_batch_pack(const int32_t* __restrict__ tile_rank, const SysDesc* __restrict__ sys,
-                 const int32_t* __restrict__ perm, const double* __restrict__ x,
-                 const double* __restrict__ y, const double* __restrict__ z,
-                 const double* __restrict__ m, float4* __restrict__ pack,
-                 dvec4* __restrict__ origin) {
-    __shared__ double red[6][kTileJ / 32];
+                 const double* __restrict__ bbox, const int32_t* __restrict__ perm,
+                 const double* __restrict__ x, const double* __restrict__ y,
+                 const double* __restrict__ z, const double* __restrict__ m,
+                 float4* __restrict__ pack, dvec4* __restrict__ origin) {
+    // The tile's bounding box is reduced in FP32 relative to the tile's first
+    // particle c (FP64); the tile origin c + float offset is exact in FP64 and
+    // the sources are then re-expressed relative to it in FP64.  Everything
+    // depends on this tile's particles only.
+    __shared__ float red[6][kTileJ / 32];
+    __shared__ double cref[3];
     const int32_t g = blockIdx.x;
-    const SysDesc& d = sys[tile_rank[g]];
+    const int32_t r = tile_rank[g];
+    const SysDesc& d = sys[r];
+    (void)bbox;
     const int32_t t = g - d.tile_off;
     const int32_t slot = t * kTileJ + threadIdx.x;
     const bool valid = slot < d.n;
     double px = 0.0, py = 0.0, pz = 0.0, pm = 0.0;
     if (valid) {
-        const int32_t p = perm[d.off + slot];
+        const int64_t p = d.off + perm[d.off + slot];  // perm: arena-relative local order
         px = x[p];
         py = y[p];
         pz = z[p];
         pm = m[p];
     }
-    double v[6];
-    v[0] = valid ? px : 1e300;
-    v[1] = valid ? py : 1e300;
-    v[2] = valid ? pz : 1e300;
-    v[3] = valid ? -px : 1e300;
-    v[4] = valid ? -py : 1e300;
-    v[5] = valid ? -pz : 1e300;
+    if (threadIdx.x == 0) {
+        cref[0] = px;
+        cref[1] = py;
+        cref[2] = pz;
+    }
+    __syncthreads();
+    const double cx = cref[0], cy = cref[1], cz = cref[2];
+    const float fx = (float)(px - cx), fy = (float)(py - cy), fz = (float)(pz - cz);
+    float v[6];
+    v[0] = valid ? fx : 3e38f;
+    v[1] = valid ? fy : 3e38f;
+    v[2] = valid ? fz : 3e38f;
+    v[3] = valid ? -fx : 3e38f;
+    v[4] = valid ? -fy : 3e38f;
+    v[5] = valid ? -fz : 3e38f;
 #pragma unroll
     for (int k = 0; k < 6; ++k)
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+        for (int o = 16; o > 0; o >>= 1) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0)
 #pragma unroll
         for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
     __syncthreads();
-    double lo[3], hi[3];
+    float lo[3], hi[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        double a = red[k][0], b = red[k + 3][0];
+        float a = red[k][0], b = red[k + 3][0];
 #pragma unroll
         for (int w = 1; w < kTileJ / 32; ++w) {
-            a = fmin(a, red[k][w]);
-            b = fmin(b, red[k + 3][w]);
+            a = fminf(a, red[k][w]);
+            b = fminf(b, red[k + 3][w]);
         }
         lo[k] = a;
         hi[k] = -b;
     }
-    const double ox = 0.5 * (lo[0] + hi[0]);
-    const double oy = 0.5 * (lo[1] + hi[1]);
-    const double oz = 0.5 * (lo[2] + hi[2]);
+    const float oxf = 0.5f * (lo[0] + hi[0]), oyf = 0.5f * (lo[1] + hi[1]), ozf = 0.5f * (lo[2] + hi[2]);
+    const double ox = cx + (double)oxf, oy = cy + (double)oyf, oz = cz + (double)ozf;
     float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
     if (valid) {
         qx = (float)(px - ox);
@@ -159,8 +314,14 @@ __global__ void __launch_bounds__(kTileJ)
     base[8 * pr + 4 + half] = qz;
     base[8 * pr + 6 + half] = qm;
     if (threadIdx.x == 0) {
-        const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
-        origin[g] = make_dvec4(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
+        // Half diagonal from the FP32 box, enlarged to cover the rounding of the
+        // relative coordinates (the near test must never under-estimate it).
+        const float ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+        const float rr = 0.5f * sqrtf(ex * ex + ey * ey + ez * ez);
+        const float amax = fmaxf(fmaxf(fabsf(lo[0]), fabsf(hi[0])),
+                                 fmaxf(fmaxf(fabsf(lo[1]), fabsf(hi[1])),
+                                       fmaxf(fabsf(lo[2]), fabsf(hi[2]))));
+        origin[g] = make_dvec4(ox, oy, oz, (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
     }
 }
 
@@ -225,7 +386,7 @@ __global__ void __launch_bounds__(kFBlock, (ACC && !POT) ? 8 : 1) k_force_batch(
             pidx[k] = -1;
             double x = 0.0, y = 0.0, z = 0.0;
             if (slot < d.n) {
-                const int32_t p = f.perm[d.off + slot];
+                const int32_t p = (int32_t)(d.off + f.perm[d.off + slot]);
                 pidx[k] = p;
                 x = f.x[p];
                 y = f.y[p];
@@ -458,11 +619,11 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
 }
 
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
-                              const int32_t* perm, const double* x, const double* y,
-                              const double* z, const double* m, float4* pack, dvec4* origin,
-                              cudaStream_t s) {
+                              const double* bbox, const int32_t* perm, const double* x,
+                              const double* y, const double* z, const double* m, float4* pack,
+                              dvec4* origin, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
-    k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, perm, x, y, z, m, pack, origin);
+    k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, bbox, perm, x, y, z, m, pack, origin);
     return cudaGetLastError();
 }
 

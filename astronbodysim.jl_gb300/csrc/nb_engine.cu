@@ -31,6 +31,7 @@
 namespace {
 
 constexpr int kTile = 256;
+constexpr int kResortEvery = 16;
 
 struct Request {
     int64_t id = 0;
@@ -61,7 +62,9 @@ struct nb_engine {
     double *x = nullptr, *y = nullptr, *z = nullptr, *vx = nullptr, *vy = nullptr, *vz = nullptr;
     double *ax = nullptr, *ay = nullptr, *az = nullptr, *pot = nullptr, *m = nullptr;
     int32_t* sysid = nullptr;
-    int32_t* perm = nullptr;
+    int32_t* perm = nullptr;    // global radix-sort result (sorted slot -> arena particle)
+    int32_t* lperm = nullptr;   // per-system Morton order, arena-relative
+    int64_t* steps_slot = nullptr;
     void* sort_scratch = nullptr;
     float4* pack = nullptr;
     nb::dvec4* origin = nullptr;
@@ -91,9 +94,12 @@ struct nb_engine {
     int32_t ntiles_total = 0;
     int32_t nitems = 0;
     double pairs_per_step = 0.0;
+    int32_t max_small_n = 0;   // largest system ordered in shared memory
+    bool global_sort = false;  // some system is too large for the shared-memory sort
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     nb_engine_stats stats{};
+    std::vector<int64_t> finished;  // ids retired since the last nb_engine_drain_done
 };
 
 namespace {
@@ -187,7 +193,7 @@ int rebuild(nb_engine* e) {
         const Request& q = e->reqs[e->slot_req[slots[r]]];
         const int64_t nt = ntiles_of(q.n);
         nb::SysDesc d{};
-        d.off = soff;
+        d.off = q.aoff;
         d.ubase = 0;
         d.n = (int32_t)q.n;
         d.tile_off = (int32_t)toff;
@@ -228,6 +234,14 @@ int rebuild(nb_engine* e) {
     e->nitems = (int32_t)items.size();
     e->high_water = hw;
     e->pairs_per_step = pairs;
+    e->max_small_n = 0;
+    e->global_sort = false;
+    for (int32_t r = 0; r < R; ++r) {
+        if (sd[r].n <= nb::batch_small_sort_limit())
+            e->max_small_n = std::max(e->max_small_n, sd[r].n);
+        else
+            e->global_sort = true;
+    }
     e->dirty = false;
     drop_graph(e);
     return NB_OK;
@@ -239,7 +253,7 @@ nb::BatchForce force_args(nb_engine* e, const int2* items, int32_t nitems) {
     f.items = items;
     f.nitems = nitems;
     f.counter = e->counter;
-    f.perm = e->perm;
+    f.perm = e->lperm;
     f.pack = e->pack;
     f.origin = e->origin;
     f.x = e->x;
@@ -255,17 +269,32 @@ nb::BatchForce force_args(nb_engine* e, const int2* items, int32_t nitems) {
     return f;
 }
 
-// Sort + pack of all running systems (enqueue only).
-cudaError_t enqueue_sort_pack(nb_engine* e, cudaStream_t s) {
-    cudaError_t r = nb::launch_batch_bbox(e->batchsys, e->nrank, e->x, e->y, e->z, e->bbox, s);
+// Sort + pack of all running systems (enqueue only).  Systems of at most
+// batch_small_sort_limit() particles are re-ordered in shared memory, one CTA
+// each, at admission (force_all) and every kResortEvery of their own steps;
+// larger systems are ordered every step by the global radix sort over the
+// arena, which runs only when such a system is resident.  Tile origins and
+// radii are recomputed from the current positions every step.
+cudaError_t enqueue_sort_pack(nb_engine* e, cudaStream_t s, bool force_all) {
+    cudaError_t r = cudaSuccess;
+    if (e->global_sort) {
+        r = nb::launch_batch_bbox(e->batchsys, e->nrank, e->x, e->y, e->z, e->bbox, s);
+        if (r != cudaSuccess) return r;
+        r = nb::launch_batch_keys(e->sysid, e->rank_of_slot, e->bbox, e->x, e->y, e->z,
+                                  e->high_water, nb::sort_keys_buffer(e->sort_scratch, e->high_water),
+                                  e->perm, s);
+        if (r != cudaSuccess) return r;
+        r = nb::launch_sort_keys(e->sort_scratch, e->high_water, e->perm, 8, s);
+        if (r != cudaSuccess) return r;
+        r = nb::launch_batch_perm_to_local(e->batchsys, e->nrank, e->perm, e->lperm, s);
+        if (r != cudaSuccess) return r;
+    }
+    r = nb::launch_batch_sort_small(e->batchsys, e->nrank, e->max_small_n, e->steps_slot,
+                                    kResortEvery, force_all ? 1 : 0, e->x, e->y, e->z, e->bbox,
+                                    e->lperm, s);
     if (r != cudaSuccess) return r;
-    r = nb::launch_batch_keys(e->sysid, e->rank_of_slot, e->bbox, e->x, e->y, e->z, e->high_water,
-                              nb::sort_keys_buffer(e->sort_scratch, e->high_water), e->perm, s);
-    if (r != cudaSuccess) return r;
-    r = nb::launch_sort_keys(e->sort_scratch, e->high_water, e->perm, 8, s);
-    if (r != cudaSuccess) return r;
-    return nb::launch_batch_pack(e->tile_rank, e->ntiles_total, e->sysdesc, e->perm, e->x, e->y, e->z,
-                                 e->m, e->pack, e->origin, s);
+    return nb::launch_batch_pack(e->tile_rank, e->ntiles_total, e->sysdesc, e->bbox, e->lperm, e->x,
+                                 e->y, e->z, e->m, e->pack, e->origin, s);
 }
 
 // One KDK step of every running system (enqueue only).
@@ -273,12 +302,14 @@ cudaError_t enqueue_step(nb_engine* e, cudaStream_t s) {
     cudaError_t r = nb::launch_batch_drift(e->x, e->y, e->z, e->vx, e->vy, e->vz, e->sysid, e->dt_slot,
                                            e->fac_step, e->high_water, s);
     if (r != cudaSuccess) return r;
-    r = enqueue_sort_pack(e, s);
+    r = enqueue_sort_pack(e, s, false);
     if (r != cudaSuccess) return r;
     r = nb::launch_force_batch(e->p.law, force_args(e, e->items, e->nitems), e->occ_acc * e->nsm, s);
     if (r != cudaSuccess) return r;
-    return nb::launch_batch_kick(e->vx, e->vy, e->vz, e->ax, e->ay, e->az, e->sysid, e->dt_slot,
-                                 e->fac_step, e->high_water, s);
+    r = nb::launch_batch_kick(e->vx, e->vy, e->vz, e->ax, e->ay, e->az, e->sysid, e->dt_slot,
+                              e->fac_step, e->high_water, s);
+    if (r != cudaSuccess) return r;
+    return nb::launch_batch_tick(e->batchsys, e->nrank, e->steps_slot, s);
 }
 
 // Admit queued requests (FIFO) while a slot and a particle range are free;
@@ -304,6 +335,7 @@ int admit(nb_engine* e, std::vector<int32_t>& admitted) {
         NE_CK(cudaMemsetAsync(e->ay + off, 0, d, e->stream));
         NE_CK(cudaMemsetAsync(e->az + off, 0, d, e->stream));
         NE_CK(nb::launch_fill_i32(e->sysid + off, q.n, slot, e->stream));
+        NE_CK(cudaMemsetAsync(e->steps_slot + slot, 0, sizeof(int64_t), e->stream));
         NE_CK(cudaStreamSynchronize(e->stream));
         q.aoff = off;
         q.slot = slot;
@@ -343,7 +375,9 @@ int start_systems(nb_engine* e, const std::vector<int32_t>& slots) {
     for (int32_t r : ranks)
         for (int32_t b = 0; b < sd[r].nblocks; ++b) items.push_back(make_int2(r, b));
     NE_CK(cudaMemcpy(e->items_new, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
-    NE_CK(enqueue_sort_pack(e, e->stream));
+    // New systems have step count 0, so they are due for ordering; the others
+    // keep their order (their schedule must not depend on admissions).
+    NE_CK(enqueue_sort_pack(e, e->stream, false));
     NE_CK(nb::launch_force_batch(e->p.law, force_args(e, e->items_new, (int32_t)items.size()),
                                  e->occ_acc * e->nsm, e->stream));
     return half_kick(e, slots, 0.5);
@@ -374,6 +408,7 @@ int retire(nb_engine* e) {
         q.state = NB_REQ_DONE;
         e->slot_req[s] = -1;
         e->stats.done += 1;
+        e->finished.push_back(q.id);
         e->dirty = true;
     }
     return NB_OK;
@@ -401,6 +436,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     }
     cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->dev);
     e->occ_acc = nb::batch_ctas_per_sm(p->law, true, false);
+    nb::prepare_batch_sort_small();
     const int64_t P = p->max_particles, S = p->max_systems;
     e->tile_cap = P / kTile + S;
     size_t off = 0;
@@ -413,6 +449,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     size_t o_d[11];
     for (int k = 0; k < 11; ++k) o_d[k] = take(dP);
     size_t o_sys = take(sizeof(int32_t) * P), o_perm = take(sizeof(int32_t) * P);
+    size_t o_lperm = take(sizeof(int32_t) * P), o_steps = take(sizeof(int64_t) * S);
     size_t o_sort = take(nb::sort_scratch_bytes(P));
     size_t o_pack = take(sizeof(float4) * kTile * (size_t)e->tile_cap);
     size_t o_orig = take(sizeof(nb::dvec4) * (size_t)e->tile_cap);
@@ -433,6 +470,8 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     for (int k = 0; k < 11; ++k) *dp[k] = (double*)(b + o_d[k]);
     e->sysid = (int32_t*)(b + o_sys);
     e->perm = (int32_t*)(b + o_perm);
+    e->lperm = (int32_t*)(b + o_lperm);
+    e->steps_slot = (int64_t*)(b + o_steps);
     e->sort_scratch = b + o_sort;
     e->pack = (float4*)(b + o_pack);
     e->origin = (nb::dvec4*)(b + o_orig);
@@ -623,6 +662,15 @@ int nb_engine_get_stats(nb_engine* e, nb_engine_stats* out) {
         }
     }
     *out = s;
+    return NB_OK;
+}
+
+int nb_engine_drain_done(nb_engine* e, int64_t* ids, int64_t cap, int64_t* count) {
+    if (!e || !count || (cap > 0 && !ids)) return NB_ERR_INVALID_ARG;
+    const int64_t k = std::min<int64_t>(cap, (int64_t)e->finished.size());
+    for (int64_t i = 0; i < k; ++i) ids[i] = e->finished[i];
+    e->finished.erase(e->finished.begin(), e->finished.begin() + k);
+    *count = k;
     return NB_OK;
 }
 

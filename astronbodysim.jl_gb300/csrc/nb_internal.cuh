@@ -146,6 +146,8 @@ struct BatchSys {
 struct BatchForce {
     const SysDesc* sys;   // by rank; off = first sorted slot
     const int2* items;    // (rank, i-block), largest systems first
+    // sys[r].off is the system's first arena particle and perm its
+    // arena-relative Morton order: slot q is particle off + perm[off + q]
     int32_t nitems;
     int32_t pad;
     int32_t* counter;     // claim counter, zeroed by the launch
@@ -174,9 +176,18 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
                               const double* x, const double* y, const double* z, int64_t n,
                               uint64_t* keys, int32_t* vals, cudaStream_t s);
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
-                              const int32_t* perm, const double* x, const double* y,
-                              const double* z, const double* m, float4* pack, dvec4* origin,
-                              cudaStream_t s);
+                              const double* bbox, const int32_t* perm, const double* x,
+                              const double* y, const double* z, const double* m, float4* pack,
+                              dvec4* origin, cudaStream_t s);
+int batch_small_sort_limit();
+cudaError_t prepare_batch_sort_small();
+cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t max_small_n,
+                                    const int64_t* steps_slot, int32_t every, int32_t force_all,
+                                    const double* x, const double* y, const double* z,
+                                    double* bbox, int32_t* lperm, cudaStream_t s);
+cudaError_t launch_batch_perm_to_local(const BatchSys* bs, int32_t nrank, const int32_t* perm,
+                                       int32_t* lperm, cudaStream_t s);
+cudaError_t launch_batch_tick(const BatchSys* bs, int32_t nrank, int64_t* steps_slot, cudaStream_t s);
 cudaError_t launch_batch_drift(double* x, double* y, double* z, const double* vx, const double* vy,
                                const double* vz, const int32_t* sysid, const double* dt_slot,
                                const double* fac_slot, int64_t n, cudaStream_t s);

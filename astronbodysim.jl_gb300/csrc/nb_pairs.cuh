@@ -100,37 +100,52 @@ __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, 
                                                   const float* yr, const float* zr,
                                                   const float* hh, const float* h2, float* ax,
                                                   float* ay, float* az, float* ap) {
-#pragma unroll 2
+    // Same packed FP32x2 arithmetic as pair_loop_fast; each source pair is then
+    // tested for r < h on both halves and, when any lane of the warp has such a
+    // pair, the spline replaces the Newtonian factor of those halves.
+    float2 nx[IPT], ny[IPT], nz[IPT];
+    float2 sx[IPT], sy[IPT], sz[IPT], sp[IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        nx[k] = make_float2(-xr[k], -xr[k]);
+        ny[k] = make_float2(-yr[k], -yr[k]);
+        nz[k] = make_float2(-zr[k], -zr[k]);
+        sx[k] = sy[k] = sz[k] = sp[k] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll 1
     for (int p = 0; p < kTileJ / 2; ++p) {
         const float4 A = b[2 * p];
         const float4 B = b[2 * p + 1];
+        const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+        const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const float4 q = half ? make_float4(A.y, A.w, B.y, B.w) : make_float4(A.x, A.z, B.x, B.z);
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const float dx = q.x - xr[k];
-                const float dy = q.y - yr[k];
-                const float dz = q.z - zr[k];
-                float r2;
-                if (LAW == NB_LAW_PLUMMER)
-                    r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, h2[k])));
-                else
-                    r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const float rinv = rsqrt_approx(r2);
-                float mp = q.w * rinv;
-                float mr3 = mp * rinv * rinv;
-                if (LAW == NB_LAW_SPLINE_G2) {
-                    if (r2 < h2[k]) spline_close(r2, rinv, q.w, hh[k], mr3, mp);
-                }
-                if (ACC) {
-                    ax[k] = fmaf(dx, mr3, ax[k]);
-                    ay[k] = fmaf(dy, mr3, ay[k]);
-                    az[k] = fmaf(dz, mr3, az[k]);
-                }
-                if (POT) ap[k] += mp;
+        for (int k = 0; k < IPT; ++k) {
+            const float2 dx = __fadd2_rn(qx, nx[k]);
+            const float2 dy = __fadd2_rn(qy, ny[k]);
+            const float2 dz = __fadd2_rn(qz, nz[k]);
+            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+            const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+            float2 mp = __fmul2_rn(qm, rinv);
+            float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
+            const bool close = (r2.x < h2[k]) | (r2.y < h2[k]);
+            if (__any_sync(0xffffffffu, close)) {
+                if (r2.x < h2[k]) spline_close(r2.x, rinv.x, qm.x, hh[k], mr3.x, mp.x);
+                if (r2.y < h2[k]) spline_close(r2.y, rinv.y, qm.y, hh[k], mr3.y, mp.y);
             }
+            if (ACC) {
+                sx[k] = __ffma2_rn(dx, mr3, sx[k]);
+                sy[k] = __ffma2_rn(dy, mr3, sy[k]);
+                sz[k] = __ffma2_rn(dz, mr3, sz[k]);
+            }
+            if (POT) sp[k] = __fadd2_rn(sp[k], mp);
         }
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        ax[k] += sx[k].x + sx[k].y;
+        ay[k] += sy[k].x + sy[k].y;
+        az[k] += sz[k].x + sz[k].y;
+        ap[k] += sp[k].x + sp[k].y;
     }
 }
 

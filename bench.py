@@ -37,7 +37,10 @@ EPS = 1.0e-3
 DT = 1.0e-4
 FLOP_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
-STEP_KERNELS = 6  # clock advance, drift, pack, force, kick, clock end
+# kernels in one step graph at N = 2^20: clock advance, drift, 2 bounding-box,
+# Morton keys, 8 radix passes x (histogram, 3-kernel scan, scatter), pack,
+# force, kick, clock end
+STEP_KERNELS = 49
 
 
 def dist_env():
@@ -280,6 +283,41 @@ def run_gpu(args):
                                 None, None, None))
     t_e2e = time.perf_counter() - t0
 
+    sim.close()
+
+    # ---- batched ensemble (many independent systems, one engine) -----------
+    batch = None
+    if not args.skip_batch:
+        ens = nb.ensemble_systems(args.batch_systems, seed=11 + rank)
+        tot = sum(d["pos"].shape[0] for d, _ in ens)
+        eng = nb.Engine(max_particles=tot + 4096, max_systems=args.batch_systems,
+                        max_steps_per_call=args.batch_steps, device=local, law=args.law)
+        for d, eps in ens:
+            eng.submit(d, eps, 1e-3, args.batch_steps)
+        del ens
+        t0 = time.perf_counter()
+        eng.run_until_idle()
+        t_batch_wall = time.perf_counter() - t0
+        st = eng.stats()
+        eng.close()
+        batch = {"value": st["interactions"] / (st["gpu_ms"] / 1e3) / 1e9, "unit": UNIT,
+                 "systems": args.batch_systems, "particles": tot, "steps": args.batch_steps,
+                 "interactions": st["interactions"], "gpu_s": st["gpu_ms"] / 1e3,
+                 "wall_s_incl_admission_and_retirement": t_batch_wall,
+                 "workload": "N log-uniform [64, 8192], half Plummer / half Hernquist (a=1, r<100a), "
+                             "m=1/N, eps U[1e-3, 1e-2], mixed, %d KDK steps dt=1e-3, one CUDA graph "
+                             "per step" % args.batch_steps}
+
+    # ---- serving sample (Poisson arrivals, continuous batching) ------------
+    serve_stats = None
+    if args.serve_seconds > 0:
+        stream = nb.RequestStream(rate=args.serve_rate, seed=7 + rank)
+        eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
+                        max_steps_per_call=args.serve_chunk, device=local, law=args.law)
+        serve_stats = nb.serve(eng, stream, args.serve_seconds, chunk_steps=args.serve_chunk)
+        eng.close()
+        serve_stats["arena_particles"] = args.serve_particles
+
     # ---- aggregate over ranks (replicas) -----------------------------------
     total_s = total_ms / 1e3
     if ws > 1:
@@ -288,6 +326,8 @@ def run_gpu(args):
         total_s, t_e2e = float(t[0]), float(t[1])
     pairs = float(n) * float(n)
     value = ws * args.steps * pairs / total_s / 1e9
+    if batch is not None:
+        batch["vs_single_system"] = batch["value"] / (value / ws)
     e2e_value = ws * args.e2e_steps * pairs / t_e2e / 1e9
 
     if rank == 0:
@@ -335,12 +375,30 @@ def run_gpu(args):
             "gpu_launches": STEP_KERNELS * args.steps,
             "clocks": clocks,
             "accuracy": acc_stats,
+            "batch": batch,
+            "serve": serve_stats,
             "wall_s_timed": t_wall,
         }
         print(json.dumps(line), flush=True)
-    sim.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_serve(args):
+    """Serving run alone (Poisson stream, continuous batching) -- one JSON line."""
+    import astronbodysim as nb
+
+    stream = nb.RequestStream(rate=args.serve_rate, seed=7)
+    eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
+                    max_steps_per_call=args.serve_chunk, law=args.law)
+    st = nb.serve(eng, stream, args.serve_seconds, chunk_steps=args.serve_chunk,
+                  log=lambda k, t: print("completed %d at %.1f s" % (k, t), file=sys.stderr)
+                  if k and k % 100 == 0 else None)
+    eng.close()
+    st.update({"mode": "serve", "rate": args.serve_rate, "arena_particles": args.serve_particles,
+               "chunk_steps": args.serve_chunk, "unit": UNIT})
+    print(json.dumps(st), flush=True)
     return 0
 
 
@@ -361,9 +419,19 @@ def main():
     ap.add_argument("--ref-targets", type=int, default=1024)
     ap.add_argument("--skip-accuracy", action="store_true")
     ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--skip-batch", action="store_true")
+    ap.add_argument("--batch-systems", type=int, default=4096)
+    ap.add_argument("--batch-steps", type=int, default=1000)
+    ap.add_argument("--serve-seconds", type=float, default=20.0)
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-chunk", type=int, default=16)
+    ap.add_argument("--serve-particles", type=int, default=1 << 22)
+    ap.add_argument("--mode", default="bench", choices=["bench", "serve"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "serve":
+        return run_serve(args)
     return run_gpu(args)
 
 

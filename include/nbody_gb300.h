@@ -250,6 +250,8 @@ int nb_batch_fetch(nb_engine *e, int64_t id, double *x, double *y, double *z, do
                    double *vy, double *vz);
 int nb_batch_cancel(nb_engine *e, int64_t id);
 int nb_engine_get_stats(nb_engine *e, nb_engine_stats *out);
+/* Ids of systems finished since the previous call (up to cap; *count set). */
+int nb_engine_drain_done(nb_engine *e, int64_t *ids, int64_t cap, int64_t *count);
 const char *nb_engine_last_error(nb_engine *e);
 
 /* Last error message of this handle (never NULL). */
