@@ -8,19 +8,23 @@ from ._lib import NbodyError, load
 from .engine import Engine
 from .serve import RequestStream, ensemble_systems, serve
 from .ics import collision, hernquist, plummer
-from .sim import (DirectSum, GPU, Simulation, active_count, advance_and_find_timestep,
-                  compute_force, compute_potential, const_step_count, diagnostics,
+from .gadget2 import internal_G, read_gadget2, write_gadget2, write_snapshot
+from .sim import (DirectSum, GPU, MOND1983Milgrom, Newton, PointMassField, PseudoNewtonianField,
+                  Simulation, active_count, advance_and_find_timestep,
+                  compute_force, compute_potential, const_step_count, counters, diagnostics,
                   drift_particles_adaptive_timestep, drift_particles_const_timestep,
                   find_min_endstep, force_and_potential_at_points, get_all_data,
-                  init_timesteps, leapfrog_half_kick, run, set_softlen, step,
+                  init_timesteps, leapfrog_half_kick, loadrestart, run, saverestart, set_softlen, step,
                   total_angular_momentum, total_energy, total_kinetic, total_momentum,
                   total_potential)
 
 __all__ = [
+    "MOND1983Milgrom", "Newton", "PointMassField", "PseudoNewtonianField",
+    "read_gadget2", "write_gadget2", "write_snapshot", "internal_G",
     "Engine", "RequestStream", "ensemble_systems", "serve", "NbodyError", "load", "plummer", "hernquist", "collision", "DirectSum", "GPU", "Simulation",
-    "active_count", "advance_and_find_timestep", "compute_force", "compute_potential",
+    "active_count", "counters", "advance_and_find_timestep", "compute_force", "compute_potential",
     "const_step_count", "diagnostics", "drift_particles_adaptive_timestep",
     "drift_particles_const_timestep", "find_min_endstep", "force_and_potential_at_points",
-    "get_all_data", "init_timesteps", "leapfrog_half_kick", "run", "set_softlen", "step",
+    "get_all_data", "saverestart", "loadrestart", "init_timesteps", "leapfrog_half_kick", "run", "set_softlen", "step",
     "total_angular_momentum", "total_energy", "total_kinetic", "total_momentum", "total_potential",
 ]

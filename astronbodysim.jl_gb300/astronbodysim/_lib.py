@@ -63,6 +63,15 @@ class nb_params(ctypes.Structure):
         ("tile_j", ctypes.c_int32),
         ("i_per_thread", ctypes.c_int32),
         ("block", ctypes.c_int32),
+        ("j_split", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("bg_kind", ctypes.c_int32),
+        ("mond", ctypes.c_int32),
+        ("bg_gm", ctypes.c_double),
+        ("bg_center", ctypes.c_double * 3),
+        ("bg_rg", ctypes.c_double),
+        ("mond_acc0", ctypes.c_double),
+        ("mond_nu_index", ctypes.c_double),
     ]
 
 
@@ -93,6 +102,12 @@ NB_REQ_QUEUED = 0
 NB_REQ_RUNNING = 1
 NB_REQ_DONE = 2
 NB_REQ_CANCELLED = 3
+NB_REQ_SUSPENDED = 4
+NB_BG_NONE = 0
+NB_BG_POINT_MASS = 1
+NB_BG_PSEUDO_NEWTONIAN = 2
+NB_MOND_NONE = 0
+NB_MOND_MILGROM1983 = 1
 
 
 class nb_diag(ctypes.Structure):
@@ -137,6 +152,12 @@ SIGNATURES = {
     "nb_get_time": (ctypes.c_int, [_h, _i64p, _dp]),
     "nb_diagnostics": (ctypes.c_int, [_h, ctypes.c_int, ctypes.POINTER(nb_diag)]),
     "nb_active_count": (ctypes.c_int, [_h, _i64p]),
+    "nb_get_counters": (ctypes.c_int, [_h, _i64p, _dp]),
+    "nb_batch_suspend": (ctypes.c_int, [_h, ctypes.c_int64]),
+    "nb_batch_resume": (ctypes.c_int, [_h, ctypes.c_int64]),
+    "nb_checkpoint_size": (ctypes.c_int, [_h, _i64p]),
+    "nb_checkpoint_save": (ctypes.c_int, [_h, _vp, ctypes.c_int64]),
+    "nb_checkpoint_load": (ctypes.c_int, [_h, _vp, ctypes.c_int64]),
     "nb_force_noalloc": (ctypes.c_int, [ctypes.c_int64, _vp, _vp, _vp, _vp, ctypes.c_int32,
                                         ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp, _vp,
                                         ctypes.c_char_p, ctypes.c_int64]),

@@ -1,0 +1,104 @@
+"""Autotuner for the force kernel's launch shape.
+
+For each particle count it times nb_compute_force (mixed precision) with
+every candidate shape -- the direct grid with (threads per CTA, targets per
+thread) in {128, 256} x {1, 2, 4}, and the persistent work-list kernel -- using
+CUDA events on the handle's stream, and records the fastest in a JSON table
+(tuning_gb300.json next to this file, or a path given by the caller).
+Simulation(tuning=...) looks the table up by the nearest particle count of the
+same law; without a table the library's built-in rule applies.
+"""
+import json
+import math
+import os
+
+import numpy as np
+
+from .ics import plummer
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_TABLE = os.path.join(HERE, "tuning_gb300.json")
+
+CANDIDATES = [
+    {"block": 128, "i_per_thread": 1, "j_split": 1},
+    {"block": 128, "i_per_thread": 2, "j_split": 1},
+    {"block": 128, "i_per_thread": 4, "j_split": 1},
+    {"block": 256, "i_per_thread": 1, "j_split": 1},
+    {"block": 256, "i_per_thread": 2, "j_split": 1},
+    {"block": 128, "i_per_thread": 1, "j_split": 2},
+    {"block": 128, "i_per_thread": 2, "j_split": 2},
+    {"block": -1, "i_per_thread": 0, "j_split": 1},  # persistent work list
+]
+
+
+def _time_force(sim, reps):
+    import torch
+
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    from .sim import compute_force
+
+    compute_force(sim)  # warm-up (also captures nothing; plain launches)
+    times = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        compute_force(sim)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return float(np.median(times))
+
+
+def tune(sizes, law="spline", reps=3, eps=1e-3, seed=0, log=print):
+    """Returns {"law": law, "entries": [{"n", "best", "ms": {shape: ms}}]}."""
+    from .sim import Simulation
+
+    entries = []
+    for n in sizes:
+        data = plummer(int(n), seed=seed)
+        res = {}
+        for c in CANDIDATES:
+            sim = Simulation(data, ForceSofteningTable=[eps] * 6, TimeStep=1e-4, precision="mixed",
+                             law=law, block=c["block"], i_per_thread=c["i_per_thread"],
+                             j_split=c["j_split"])
+            key = "worklist" if c["block"] == -1 else "%dx%dx%d" % (c["block"], c["i_per_thread"],
+                                                                    c["j_split"])
+            res[key] = _time_force(sim, reps)
+            sim.close()
+        best = min(res, key=res.get)
+        entries.append({"n": int(n), "best": best, "ms": res,
+                        "g_interactions_per_s": float(n) * n / (res[best] / 1e3) / 1e9})
+        if log:
+            log("n=%d best=%s %.3f ms (%s)" % (n, best, res[best],
+                                               ", ".join("%s %.3f" % kv for kv in res.items())))
+    return {"law": law, "entries": entries}
+
+
+def save(table, path=DEFAULT_TABLE):
+    old = load(path) or {}
+    old[table["law"]] = table["entries"]
+    with open(path, "w") as f:
+        json.dump(old, f, indent=1, sort_keys=True)
+
+
+def load(path=DEFAULT_TABLE):
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
+
+
+def lookup(n, law="spline", path=DEFAULT_TABLE):
+    """(block, i_per_thread, j_split) of the tuned shape nearest to n in log
+    space, or None."""
+    t = load(path)
+    if not t or law not in t or not t[law]:
+        return None
+    e = min(t[law], key=lambda e: abs(math.log(e["n"]) - math.log(max(1, n))))
+    best = e["best"]
+    if best == "worklist":
+        return -1, 0, 0
+    b, i, j = best.split("x")
+    return int(b), int(i), int(j)

@@ -91,6 +91,14 @@ class Engine:
     def cancel(self, rid):
         self._ck(self._lib.nb_batch_cancel(self.handle, int(rid)))
 
+    def suspend(self, rid):
+        """Evict a running system to host memory (nb_batch_suspend)."""
+        self._ck(self._lib.nb_batch_suspend(self.handle, int(rid)))
+
+    def resume(self, rid):
+        """Queue a suspended system again (nb_batch_resume)."""
+        self._ck(self._lib.nb_batch_resume(self.handle, int(rid)))
+
     def drain_done(self, cap=4096):
         """Ids of systems finished since the previous call."""
         out = []

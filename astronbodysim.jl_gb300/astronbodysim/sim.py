@@ -37,6 +37,40 @@ class DirectSum:
     """Gravity solver trait (src/base/Traits.jl)."""
 
 
+class Newton:
+    """Gravity model trait (src/base/Traits.jl): plain Newtonian forces."""
+
+
+class MOND1983Milgrom:
+    """Gravity model trait: Newtonian forces scaled by the Milgrom (1983)
+    interpolation nu(|a| / ACC0, MOND_nuIndex) (src/mond/milgrom1983.jl)."""
+
+
+class PointMassField:
+    """Background force of a point mass: a += -GM / |r|^2 * r / |r|, r = x -
+    center (the attractor closure of test/Local-Timestep.jl:746)."""
+
+    kind = L.NB_BG_POINT_MASS
+
+    def __init__(self, GM, center=(0.0, 0.0, 0.0)):
+        self.GM, self.center, self.rg = float(GM), tuple(float(c) for c in center), 0.0
+
+
+class PseudoNewtonianField:
+    """Background force of a compact object in the pseudo-Newtonian potential:
+    a += -GM / (|r| - r_g)^2 * r / |r| (src/tools/BlackHole.jl:41-60)."""
+
+    kind = L.NB_BG_PSEUDO_NEWTONIAN
+
+    def __init__(self, GM, rg, center=(0.0, 0.0, 0.0)):
+        self.GM, self.center, self.rg = float(GM), tuple(float(c) for c in center), float(rg)
+
+
+# Checkpoint image header: magic[8], version, n, bytes, params_size, clock_size
+# (int64 each), then nb_params.
+_CKPT_PARAMS_OFFSET = 48
+
+
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
@@ -53,7 +87,8 @@ class Simulation:
     def __init__(self, data, *, G=1.0, ForceSofteningTable=None, TimeStep=0.0, TimeBegin=0.0,
                  TimeEnd=0.1, TimeBase=1 << 30, ErrTolTimestep=0.025, MinStep=1.0e-8,
                  MaxStep=float("inf"), law="spline", precision="mixed", criterion="ref",
-                 device=None, block=0, i_per_thread=0):
+                 device=None, block=0, i_per_thread=0, j_split=0, tuning=None, bgforce=None,
+                 GravityModel=None, ACC0=0.0, MOND_nuIndex=2.0):
         self._lib = L.load()
         p = L.nb_params()
         self._lib.nb_default_params(ctypes.byref(p))
@@ -76,8 +111,33 @@ class Simulation:
         p.time_begin = float(TimeBegin)
         p.time_end = float(TimeEnd)
         p.device = (device.id if isinstance(device, GPU) else int(device or 0))
+        # force post-processing (postprocessing_force, src/directsumgpu/gravity.jl:64-79)
+        fields = list(bgforce) if isinstance(bgforce, (list, tuple)) else ([bgforce] if bgforce else [])
+        if len(fields) > 1:
+            raise ValueError("one analytic background field per simulation")
+        if fields:
+            f = fields[0]
+            p.bg_kind, p.bg_gm, p.bg_rg = f.kind, f.GM, f.rg
+            for k in range(3):
+                p.bg_center[k] = f.center[k]
+        if GravityModel is not None and (GravityModel is MOND1983Milgrom or
+                                          isinstance(GravityModel, MOND1983Milgrom)):
+            p.mond = L.NB_MOND_MILGROM1983
+            p.mond_acc0 = float(ACC0)
+            p.mond_nu_index = float(MOND_nuIndex)
+        if tuning and not block and not i_per_thread and data is not None:
+            # launch shape from the autotuner's table (nearest particle count)
+            from . import autotune
+
+            path = autotune.DEFAULT_TABLE if tuning == "auto" else tuning
+            n0 = np.asarray(data["pos"]).reshape(-1, 3).shape[0]
+            shape = autotune.lookup(n0, law=law, path=path)
+            if shape:
+                block, i_per_thread, j_split = shape
         p.block = int(block)
         p.i_per_thread = int(i_per_thread)
+        p.j_split = int(j_split)
+        self.tuned_shape = (int(block), int(i_per_thread), int(j_split))
         self.params = p
         self.G = float(G)
         self.softening = [float(s) for s in soft]
@@ -131,6 +191,42 @@ class Simulation:
                                      L.i32ptr(ctype)))
         self.n = n
         self.mass = mass
+        self.collection = (np.ones(n, dtype=np.int32) if ctype is None else ctype.copy())
+
+    # -- checkpoint / restart ----------------------------------------------
+    def checkpoint(self):
+        """Image (bytes) of the device state: parameters, particles (x, v, a,
+        pot, m, type, Ti_begstep, Ti_endstep) and the device time line
+        (nb_checkpoint_save)."""
+        nbytes = ctypes.c_int64()
+        self._ck(self._lib.nb_checkpoint_size(self.handle, ctypes.byref(nbytes)))
+        buf = np.empty(nbytes.value, dtype=np.uint8)
+        self._ck(self._lib.nb_checkpoint_save(self.handle, buf.ctypes.data_as(ctypes.c_void_p),
+                                              nbytes.value))
+        return buf.tobytes()
+
+    def restore(self, image):
+        """Loads a checkpoint image into this handle (nb_checkpoint_load); the
+        run continues bit-identically to the one that was saved."""
+        buf = np.frombuffer(image, dtype=np.uint8)
+        self._ck(self._lib.nb_checkpoint_load(self.handle, buf.ctypes.data_as(ctypes.c_void_p),
+                                              buf.size))
+        p = L.nb_params.from_buffer_copy(image, _CKPT_PARAMS_OFFSET)
+        n = int(np.frombuffer(image, dtype=np.int64, count=1, offset=16)[0])
+        arrays = 11 * 8 * n + (4 * n + 7) // 8 * 8 + 16 * n
+        hdr = len(image) - arrays
+        self.params = p
+        self.G = p.G
+        self.softening = list(p.softening)
+        self.TimeBegin, self.TimeEnd = p.time_begin, p.time_end
+        self.TimeStep = p.dt if not p.adaptive else 0.0
+        self.TimeBase = int(p.time_base)
+        self.adaptive = bool(p.adaptive)
+        self.TimeInterval = (self.TimeEnd - self.TimeBegin) / self.TimeBase
+        self.n = n
+        self.mass = np.frombuffer(image, dtype=np.float64, count=n, offset=hdr + 10 * 8 * n).copy()
+        self.collection = np.frombuffer(image, dtype=np.int32, count=n,
+                                        offset=hdr + 11 * 8 * n).copy()
 
     def set_stream(self, stream_ptr):
         self._ck(self._lib.nb_set_stream(self.handle, ctypes.c_void_p(stream_ptr)))
@@ -178,6 +274,31 @@ class Simulation:
 # ---------------------------------------------------------------------------
 # Reference-named operations
 # ---------------------------------------------------------------------------
+
+def saverestart(sim, filename):
+    """saverestart for (DirectSum, GPU) (src/restart.jl:14-19): the device state
+    written to one file."""
+    with open(filename, "wb") as f:
+        f.write(sim.checkpoint())
+
+
+def loadrestart(filename, device=None):
+    """loadrestart (src/restart.jl:129-139): a new Simulation on `device`
+    (default: the saved one) holding the saved state."""
+    with open(filename, "rb") as f:
+        image = f.read()
+    p = L.nb_params.from_buffer_copy(image, _CKPT_PARAMS_OFFSET)
+    inv = lambda d, v: next(k for k, x in d.items() if x == v)  # noqa: E731
+    sim = Simulation(None, G=p.G, ForceSofteningTable=list(p.softening),
+                     TimeStep=p.dt if not p.adaptive else 0.0, TimeBegin=p.time_begin,
+                     TimeEnd=p.time_end, TimeBase=p.time_base, ErrTolTimestep=p.eta,
+                     MinStep=p.min_step, MaxStep=p.max_step, law=inv(LAWS, p.law),
+                     precision=inv(PRECISIONS, p.precision), criterion=inv(CRITERIA, p.criterion),
+                     device=p.device if device is None else device, block=p.block,
+                     i_per_thread=p.i_per_thread, j_split=p.j_split)
+    sim.restore(image)
+    return sim
+
 
 def get_all_data(sim):
     """src/base/Config.jl:1228-1230 (download to host)."""
@@ -252,6 +373,14 @@ def drift_particles_const_timestep(sim, next_float):
 def step(sim, nsteps=1):
     """step(sim, DirectSum, GPU) repeated nsteps times (CUDA-graph replay)."""
     sim._ck(sim._lib.nb_step(sim.handle, int(nsteps)))
+
+
+def counters(sim):
+    """(steps taken by step(), pair evaluations they made)."""
+    k = ctypes.c_int64()
+    v = ctypes.c_double()
+    sim._ck(sim._lib.nb_get_counters(sim.handle, ctypes.byref(k), ctypes.byref(v)))
+    return k.value, v.value
 
 
 def active_count(sim):

@@ -54,6 +54,9 @@ struct nb_handle {
     nb::SysDesc* sysdesc = nullptr;
     float* partial = nullptr;
     size_t partial_bytes = 0;
+    int jsplit = 1;
+    float* jpartial = nullptr;  // j-split partials (arena)
+    int64_t jstride = 0;
     std::string err;
 };
 
@@ -122,6 +125,16 @@ int check_params(nb_handle* h, const nb_params* p) {
         return fail(h, NB_ERR_INVALID_ARG, "block must be 0 (auto), -1 (work list), 128 or 256");
     if (i != 0 && i != 1 && i != 2 && i != 4)
         return fail(h, NB_ERR_INVALID_ARG, "i_per_thread must be 1, 2 or 4");
+    if (p->bg_kind < NB_BG_NONE || p->bg_kind > NB_BG_PSEUDO_NEWTONIAN || !std::isfinite(p->bg_gm) ||
+        !std::isfinite(p->bg_rg) || !std::isfinite(p->bg_center[0]) ||
+        !std::isfinite(p->bg_center[1]) || !std::isfinite(p->bg_center[2]))
+        return fail(h, NB_ERR_INVALID_ARG, "bad background field parameters");
+    if (p->mond != NB_MOND_NONE &&
+        (p->mond != NB_MOND_MILGROM1983 || !(p->mond_acc0 > 0.0) || !std::isfinite(p->mond_acc0) ||
+         !(p->mond_nu_index > 0.0) || !std::isfinite(p->mond_nu_index)))
+        return fail(h, NB_ERR_INVALID_ARG, "MOND needs ACC0 > 0 and MOND_nuIndex > 0");
+    if (p->j_split < 0 || p->j_split > 4)
+        return fail(h, NB_ERR_INVALID_ARG, "j_split must be 0..4");
     if (p->tile_j != 0 && p->tile_j != kTileJ)
         return fail(h, NB_ERR_INVALID_ARG, "tile_j must be %d", kTileJ);
     return NB_OK;
@@ -252,7 +265,30 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
         }
     }
     nb::Sources32 src{h->pack, h->origin, h->ntiles, kTileJ};
+    if (particles && h->jsplit > 1) {
+        src.jsplit = h->jsplit;
+        src.partial = h->jpartial;
+        src.pstride = h->jstride;
+    }
     return nb::launch_force_mixed(h->p.law, pot, src, t2, h->p.G, &h->clk->err, blk, ipt, s);
+}
+
+// Force post-processing of the particles that received a force (no-op when
+// neither a background field nor MOND is configured).
+cudaError_t enqueue_post(nb_handle* h, cudaStream_t s, bool active_only) {
+    if (h->p.bg_kind == NB_BG_NONE && h->p.mond == NB_MOND_NONE) return cudaSuccess;
+    nb::PostCfg c{};
+    c.bg_kind = h->p.bg_kind;
+    c.mond = h->p.mond;
+    c.gm = h->p.bg_gm;
+    c.cx = h->p.bg_center[0];
+    c.cy = h->p.bg_center[1];
+    c.cz = h->p.bg_center[2];
+    c.rg = h->p.bg_rg;
+    c.acc0 = h->p.mond_acc0;
+    c.nu_index = h->p.mond_nu_index;
+    return nb::launch_postprocess(h->ax, h->ay, h->az, h->x, h->y, h->z, h->ti_end, h->n, h->clk,
+                                  active_only ? 1 : 0, c, s);
 }
 
 // Enqueue step(sim, DirectSum, GPU): drift -> force(active) -> kick.
@@ -272,10 +308,12 @@ cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
     }
     e = enqueue_force(h, particle_targets(h, true, false), s, adaptive);
     if (e != cudaSuccess) return e;
+    e = enqueue_post(h, s, adaptive);
+    if (e != cudaSuccess) return e;
     e = nb::launch_kick(h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->type, h->ti_beg, h->ti_end,
                         h->n, h->tc, h->clk, s);
     if (e != cudaSuccess) return e;
-    return nb::launch_clock_end_step(h->clk, h->p.adaptive, s);
+    return nb::launch_clock_end_step(h->clk, h->p.adaptive, h->n, s);
 }
 
 int ensure_capacity(nb_handle* h, int64_t n) {
@@ -303,6 +341,9 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     size_t o_tb = take(sizeof(int64_t) * (size_t)n), o_te = take(sizeof(int64_t) * (size_t)n);
     size_t o_act = take(sizeof(int32_t) * (size_t)n);
     size_t o_perm = take(sizeof(int32_t) * (size_t)n);
+    // j-split partials: jsplit x 8 floats per target slot (slots padded to 1024)
+    const int64_t jstride = (n + 1023) / 1024 * 1024;
+    size_t o_jp = take(h->jsplit > 1 ? sizeof(float) * 8 * (size_t)h->jsplit * jstride : 0);
     size_t o_acts = take(sizeof(uint32_t) * (size_t)nb::active_scratch_words(n));
     size_t o_sort = take(nb::sort_scratch_bytes(n));
     size_t o_pack = take(sizeof(float4) * (size_t)npad);
@@ -330,6 +371,8 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->ti_end = (int64_t*)(b + o_te);
     h->active = (int32_t*)(b + o_act);
     h->perm = (int32_t*)(b + o_perm);
+    h->jpartial = h->jsplit > 1 ? (float*)(b + o_jp) : nullptr;
+    h->jstride = jstride;
     h->act_scratch = (uint32_t*)(b + o_acts);
     h->sort_scratch = (void*)(b + o_sort);
     h->pack = (float4*)(b + o_pack);
@@ -355,6 +398,35 @@ int upload_sysdesc(nb_handle* h) {
     for (int k = 0; k < 6; ++k) d.soft[k] = h->p.softening[k];
     NB_CK(cudaMemcpy(h->sysdesc, &d, sizeof d, cudaMemcpyHostToDevice));
     return NB_OK;
+}
+
+// Launch-shape choice of nb_params (block, i_per_thread, j_split).
+void apply_tuning(nb_handle* h, const nb_params& p) {
+    h->block = p.block > 0 ? p.block : 128;
+    h->ipt = p.i_per_thread ? p.i_per_thread : 2;
+    h->jsplit = p.j_split > 1 ? p.j_split : 1;
+    h->worklist = p.block == -1;
+    h->auto_cfg = p.block == 0 && p.i_per_thread == 0;
+}
+
+// Checkpoint image: this header, then x, y, z, vx, vy, vz, ax, ay, az, pot, m
+// (FP64, n each), type (int32, n, padded to 8 bytes), Ti_begstep, Ti_endstep
+// (int64, n each).
+struct CkptHeader {
+    char magic[8];
+    int64_t version;
+    int64_t n;
+    int64_t bytes;
+    int64_t params_size;
+    int64_t clock_size;
+    nb_params p;
+    Clock clk;
+};
+constexpr char kCkptMagic[8] = {'N', 'B', 'G', 'B', '3', '0', '0', 'C'};
+constexpr int64_t kCkptVersion = 1;
+
+int64_t ckpt_bytes(int64_t n) {
+    return (int64_t)sizeof(CkptHeader) + 11 * 8 * n + (int64_t)align_up(4 * (size_t)n, 8) + 16 * n;
 }
 
 int require_particles(nb_handle* h) {
@@ -390,6 +462,7 @@ void nb_default_params(nb_params* p) {
     p->time_begin = 0.0;
     p->time_end = 0.1;
     p->device = 0;
+    p->mond_nu_index = 2.0;
 }
 
 int nb_create(const nb_params* p, nb_handle** out) {
@@ -410,8 +483,6 @@ int nb_create(const nb_params* p, nb_handle** out) {
     h->p = *p;
     h->tc = make_timecfg(*p);
     h->dev = p->device;
-    h->block = p->block ? p->block : 128;
-    h->ipt = p->i_per_thread ? p->i_per_thread : 2;
     if (cudaSetDevice(h->dev) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&h->clk, sizeof(Clock)) != cudaSuccess) {
@@ -428,9 +499,7 @@ int nb_create(const nb_params* p, nb_handle** out) {
     // the partial-sum scratch is sized for the largest grid.
     // block == -1: persistent work-list kernel; block/ipt given: direct grid with
     // that shape; 0/0: chosen per particle count in enqueue_force.
-    h->worklist = p->block == -1;
-    h->auto_cfg = p->block == 0 && p->i_per_thread == 0;
-    if (p->block == -1) h->block = 128;
+    apply_tuning(h, *p);
     cudaDeviceGetAttribute(&h->nsm, cudaDevAttrMultiProcessorCount, h->dev);
     int occ_max = 0;
     for (int law = 0; law < 2; ++law)
@@ -507,6 +576,8 @@ int nb_upload(nb_handle* h, int64_t n, const double* x, const double* y, const d
         if (rc) return rc;
     }
     h->n = n;
+    // tiles of this upload (the arena may hold more from a larger earlier one)
+    h->ntiles = (int32_t)((n + kTileJ - 1) / kTileJ);
     drop_graph(h);
     if (n == 0) return NB_OK;
     const size_t d = sizeof(double) * (size_t)n;
@@ -615,6 +686,7 @@ int nb_compute_force(nb_handle* h, int flags) {
     const bool adaptive = h->p.adaptive != 0;
     NB_CK(enqueue_force(h, particle_targets(h, true, (flags & NB_FORCE_POT) != 0), h->stream,
                         adaptive));
+    NB_CK(enqueue_post(h, h->stream, adaptive));
     return sync_and_check(h);
 }
 
@@ -809,6 +881,18 @@ int nb_get_time(nb_handle* h, int64_t* t_int, double* t_float) {
     return NB_OK;
 }
 
+int nb_get_counters(nb_handle* h, int64_t* steps, double* interactions) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    Clock c{};
+    NB_CK(cudaStreamSynchronize(h->stream));
+    NB_CK(cudaMemcpy(&c, h->clk, sizeof c, cudaMemcpyDeviceToHost));
+    if (steps) *steps = c.steps;
+    if (interactions) *interactions = c.interactions;
+    return NB_OK;
+}
+
 int nb_diagnostics(nb_handle* h, int with_potential, nb_diag* out) {
     if (!h || !out) return NB_ERR_INVALID_ARG;
     int rc = use_device(h);
@@ -845,6 +929,110 @@ int nb_active_count(nb_handle* h, int64_t* count) {
     NB_CK(cudaStreamSynchronize(h->stream));
     *count = c;
     return NB_OK;
+}
+
+int nb_checkpoint_size(nb_handle* h, int64_t* bytes) {
+    if (!h || !bytes) return NB_ERR_INVALID_ARG;
+    *bytes = ckpt_bytes(h->n);
+    return NB_OK;
+}
+
+int nb_checkpoint_save(nb_handle* h, void* buf, int64_t bytes) {
+    if (!h || !buf) return fail(h, NB_ERR_INVALID_ARG, "null checkpoint buffer");
+    const int64_t n = h->n;
+    if (bytes < ckpt_bytes(n))
+        return fail(h, NB_ERR_INVALID_ARG, "checkpoint buffer of %lld bytes, need %lld",
+                    (long long)bytes, (long long)ckpt_bytes(n));
+    int rc = use_device(h);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    NB_CK(cudaStreamSynchronize(s));
+    CkptHeader hd{};
+    std::memcpy(hd.magic, kCkptMagic, sizeof hd.magic);
+    hd.version = kCkptVersion;
+    hd.n = n;
+    hd.bytes = ckpt_bytes(n);
+    hd.params_size = (int64_t)sizeof(nb_params);
+    hd.clock_size = (int64_t)sizeof(Clock);
+    hd.p = h->p;
+    NB_CK(cudaMemcpy(&hd.clk, h->clk, sizeof(Clock), cudaMemcpyDeviceToHost));
+    char* b = static_cast<char*>(buf);
+    std::memcpy(b, &hd, sizeof hd);
+    size_t off = sizeof hd;
+    if (n > 0) {
+        const double* arrs[11] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->pot, h->m};
+        const size_t d = sizeof(double) * (size_t)n;
+        for (const double* a : arrs) {
+            NB_CK(cudaMemcpyAsync(b + off, a, d, cudaMemcpyDeviceToHost, s));
+            off += d;
+        }
+        NB_CK(cudaMemcpyAsync(b + off, h->type, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        off += align_up(4 * (size_t)n, 8);
+        NB_CK(cudaMemcpyAsync(b + off, h->ti_beg, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        off += sizeof(int64_t) * (size_t)n;
+        NB_CK(cudaMemcpyAsync(b + off, h->ti_end, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        NB_CK(cudaStreamSynchronize(s));
+    }
+    return NB_OK;
+}
+
+int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
+    if (!h || !buf) return fail(h, NB_ERR_INVALID_ARG, "null checkpoint buffer");
+    if (bytes < (int64_t)sizeof(CkptHeader))
+        return fail(h, NB_ERR_INVALID_ARG, "checkpoint image too short");
+    CkptHeader hd;
+    std::memcpy(&hd, buf, sizeof hd);
+    if (std::memcmp(hd.magic, kCkptMagic, sizeof hd.magic) != 0 || hd.version != kCkptVersion ||
+        hd.params_size != (int64_t)sizeof(nb_params) || hd.clock_size != (int64_t)sizeof(Clock))
+        return fail(h, NB_ERR_INVALID_ARG, "not a checkpoint image of this library version");
+    const int64_t n = hd.n;
+    if (n < 0 || n > (int64_t)0x7fffffff || hd.bytes != ckpt_bytes(n) || bytes < hd.bytes)
+        return fail(h, NB_ERR_INVALID_ARG, "checkpoint image size does not match its particle count");
+    nb_params p = hd.p;
+    p.device = h->dev;  // the image moves to this handle's device
+    int rc = check_params(h, &p);
+    if (rc) return rc;
+    const char* b = static_cast<const char*>(buf);
+    const int32_t* type = reinterpret_cast<const int32_t*>(b + sizeof hd + 11 * 8 * (size_t)n);
+    for (int64_t i = 0; i < n; ++i)
+        if (type[i] < 1 || type[i] > 6)
+            return fail(h, NB_ERR_INVALID_ARG, "checkpoint type[%lld]=%d outside 1..6", (long long)i, type[i]);
+    rc = use_device(h);
+    if (rc) return rc;
+    cudaStream_t s = h->stream;
+    NB_CK(cudaStreamSynchronize(s));
+    drop_graph(h);
+    const int old_js = h->jsplit;
+    h->p = p;
+    h->tc = make_timecfg(p);
+    apply_tuning(h, p);
+    if (h->jsplit != old_js && h->arena) {  // the arena layout depends on j_split
+        NB_CK(cudaFree(h->arena));
+        h->arena = nullptr;
+        h->cap = 0;
+    }
+    if (n > 0) {
+        rc = ensure_capacity(h, n);
+        if (rc) return rc;
+    }
+    h->n = n;
+    h->ntiles = (int32_t)((n + kTileJ - 1) / kTileJ);
+    NB_CK(cudaMemcpy(h->clk, &hd.clk, sizeof(Clock), cudaMemcpyHostToDevice));
+    if (n == 0) return NB_OK;
+    size_t off = sizeof hd;
+    double* arrs[11] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->pot, h->m};
+    const size_t d = sizeof(double) * (size_t)n;
+    for (double* a : arrs) {
+        NB_CK(cudaMemcpyAsync(a, b + off, d, cudaMemcpyHostToDevice, s));
+        off += d;
+    }
+    NB_CK(cudaMemcpyAsync(h->type, b + off, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s));
+    off += align_up(4 * (size_t)n, 8);
+    NB_CK(cudaMemcpyAsync(h->ti_beg, b + off, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, s));
+    off += sizeof(int64_t) * (size_t)n;
+    NB_CK(cudaMemcpyAsync(h->ti_end, b + off, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, s));
+    NB_CK(cudaStreamSynchronize(s));
+    return upload_sysdesc(h);
 }
 
 const char* nb_last_error(nb_handle* h) {

@@ -45,6 +45,9 @@ struct Request {
     int32_t state = NB_REQ_QUEUED;
     int32_t slot = -1;
     int64_t aoff = -1;
+    // suspended state: in = x, y, z, vx, vy, vz, m, ax, ay, az (n each), order = lperm
+    bool resumed = false;
+    std::vector<int32_t> order;
 };
 
 }  // namespace
@@ -328,23 +331,35 @@ int admit(nb_engine* e, std::vector<int32_t>& admitted) {
         if (off < 0) break;  // head of the queue waits for space (FIFO)
         const size_t d = sizeof(double) * (size_t)q.n;
         const double* in = q.in.data();
-        double* dst[7] = {e->x, e->y, e->z, e->vx, e->vy, e->vz, e->m};
-        for (int k = 0; k < 7; ++k)
+        double* dst[10] = {e->x, e->y, e->z, e->vx, e->vy, e->vz, e->m, e->ax, e->ay, e->az};
+        const int narr = q.resumed ? 10 : 7;
+        for (int k = 0; k < narr; ++k)
             NE_CK(cudaMemcpyAsync(dst[k] + off, in + (size_t)k * q.n, d, cudaMemcpyHostToDevice, e->stream));
-        NE_CK(cudaMemsetAsync(e->ax + off, 0, d, e->stream));
-        NE_CK(cudaMemsetAsync(e->ay + off, 0, d, e->stream));
-        NE_CK(cudaMemsetAsync(e->az + off, 0, d, e->stream));
+        if (q.resumed) {
+            // own Morton order and step count, so the re-ordering schedule continues
+            NE_CK(cudaMemcpyAsync(e->lperm + off, q.order.data(), sizeof(int32_t) * (size_t)q.n,
+                                  cudaMemcpyHostToDevice, e->stream));
+            NE_CK(cudaMemcpyAsync(e->steps_slot + slot, &q.steps_done, sizeof(int64_t),
+                                  cudaMemcpyHostToDevice, e->stream));
+        } else {
+            NE_CK(cudaMemsetAsync(e->ax + off, 0, d, e->stream));
+            NE_CK(cudaMemsetAsync(e->ay + off, 0, d, e->stream));
+            NE_CK(cudaMemsetAsync(e->az + off, 0, d, e->stream));
+            NE_CK(cudaMemsetAsync(e->steps_slot + slot, 0, sizeof(int64_t), e->stream));
+        }
         NE_CK(nb::launch_fill_i32(e->sysid + off, q.n, slot, e->stream));
-        NE_CK(cudaMemsetAsync(e->steps_slot + slot, 0, sizeof(int64_t), e->stream));
         NE_CK(cudaStreamSynchronize(e->stream));
         q.aoff = off;
         q.slot = slot;
         q.state = NB_REQ_RUNNING;
         q.in.clear();
         q.in.shrink_to_fit();
+        q.order.clear();
+        q.order.shrink_to_fit();
         e->slot_req[slot] = q.id;
         e->queue.pop_front();
-        admitted.push_back(slot);
+        if (!q.resumed) admitted.push_back(slot);  // a resumed system needs no start-up
+        q.resumed = false;
         e->dirty = true;
     }
     return NB_OK;
@@ -644,6 +659,48 @@ int nb_batch_cancel(nb_engine* e, int64_t id) {
         e->dirty = true;
     }
     q.state = NB_REQ_CANCELLED;
+    return NB_OK;
+}
+
+int nb_batch_suspend(nb_engine* e, int64_t id) {
+    if (!e) return NB_ERR_INVALID_ARG;
+    auto it = e->reqs.find(id);
+    if (it == e->reqs.end()) return efail(e, NB_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
+    Request& q = it->second;
+    if (q.state != NB_REQ_RUNNING)
+        return efail(e, NB_ERR_STATE, "request %lld is not running", (long long)id);
+    NE_CK(cudaSetDevice(e->dev));
+    NE_CK(cudaStreamSynchronize(e->stream));
+    q.in.resize((size_t)10 * q.n);
+    q.order.resize((size_t)q.n);
+    const size_t d = sizeof(double) * (size_t)q.n;
+    const double* src[10] = {e->x, e->y, e->z, e->vx, e->vy, e->vz, e->m, e->ax, e->ay, e->az};
+    for (int k = 0; k < 10; ++k)
+        NE_CK(cudaMemcpyAsync(q.in.data() + (size_t)k * q.n, src[k] + q.aoff, d,
+                              cudaMemcpyDeviceToHost, e->stream));
+    NE_CK(cudaMemcpyAsync(q.order.data(), e->lperm + q.aoff, sizeof(int32_t) * (size_t)q.n,
+                          cudaMemcpyDeviceToHost, e->stream));
+    NE_CK(nb::launch_fill_i32(e->sysid + q.aoff, q.n, -1, e->stream));
+    NE_CK(cudaStreamSynchronize(e->stream));
+    free_range(e, q.aoff, q.n);
+    e->slot_req[q.slot] = -1;
+    q.slot = -1;
+    q.aoff = -1;
+    q.state = NB_REQ_SUSPENDED;
+    e->dirty = true;
+    return NB_OK;
+}
+
+int nb_batch_resume(nb_engine* e, int64_t id) {
+    if (!e) return NB_ERR_INVALID_ARG;
+    auto it = e->reqs.find(id);
+    if (it == e->reqs.end()) return efail(e, NB_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
+    Request& q = it->second;
+    if (q.state != NB_REQ_SUSPENDED)
+        return efail(e, NB_ERR_STATE, "request %lld is not suspended", (long long)id);
+    q.state = NB_REQ_QUEUED;
+    q.resumed = true;
+    e->queue.push_back(id);
     return NB_OK;
 }
 

@@ -141,11 +141,15 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
     __shared__ double tpx[BLOCK * IPT], tpy[BLOCK * IPT], tpz[BLOCK * IPT];
 
     const int64_t ntg = tg.d_count ? (int64_t)(*tg.d_count) : tg.n;
-    const int64_t base = (int64_t)blockIdx.x * (BLOCK * IPT);
+    const int js = src.jsplit > 1 ? src.jsplit : 1;
+    const int64_t blk = (int64_t)blockIdx.x / js;
+    const int part = (int)(blockIdx.x % js);
+    const int64_t base = blk * (BLOCK * IPT);
     if (base >= ntg) return;  // CTA-uniform
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    const int ntiles = src.ntiles;
+    const int t_lo = (int)((int64_t)part * src.ntiles / js);
+    const int ntiles = (int)((int64_t)(part + 1) * src.ntiles / js) - t_lo;  // tiles of this CTA
 
     if (tid == 0) {
 #pragma unroll
@@ -182,7 +186,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
     if (tid == 0) {
         for (int s = 0; s < kStages && s < ntiles; ++s) {
             mbar_arrive_expect_tx(&full[s], kTileJ * sizeof(float4));
-            bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)s * kTileJ, kTileJ * sizeof(float4),
+            bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)(t_lo + s) * kTileJ, kTileJ * sizeof(float4),
                      &full[s]);
         }
     }
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
     for (int t = 0; t < ntiles; ++t) {
         const int s = t % kStages;
         const uint32_t par = (uint32_t)(t / kStages) & 1u;
-        const dvec4 o = src.origin[t];
+        const dvec4 o = src.origin[t_lo + t];
         float xr[IPT], yr[IPT], zr[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
@@ -250,7 +254,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
                 done[s] = 0;
                 if (t + kStages < ntiles) {
                     mbar_arrive_expect_tx(&full[s], kTileJ * sizeof(float4));
-                    bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)(t + kStages) * kTileJ,
+                    bulk_g2s(&buf[s * kTileJ], src.pack + (int64_t)(t_lo + t + kStages) * kTileJ,
                              kTileJ * sizeof(float4), &full[s]);
                 }
             }
@@ -276,6 +280,23 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
         return;
     }
 
+    if (js > 1) {
+        // j-split: compensated partials of this CTA's tile range
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) {
+            const int64_t slot = base + k * BLOCK + tid;
+            float* q = src.partial + (int64_t)part * 8 * src.pstride + slot;
+            q[0 * src.pstride] = sx[k];
+            q[1 * src.pstride] = cx[k];
+            q[2 * src.pstride] = sy[k];
+            q[3 * src.pstride] = cy[k];
+            q[4 * src.pstride] = sz[k];
+            q[5 * src.pstride] = cz[k];
+            q[6 * src.pstride] = sp[k];
+            q[7 * src.pstride] = cp[k];
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         const int32_t p = pidx[k];
@@ -298,12 +319,56 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
     }
 }
 
+// Adds the j-split partials of every target in part order (deterministic).
+template <int LAW, bool ACC, bool POT>
+__global__ void __launch_bounds__(256) k_force_join(Sources32 src, Targets tg, double G) {
+    const int64_t ntg = tg.d_count ? (int64_t)(*tg.d_count) : tg.n;
+    const int64_t slot = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    if (slot >= ntg) return;
+    const int32_t p = tg.idx ? tg.idx[slot] : (int32_t)slot;
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int part = 0; part < src.jsplit; ++part) {
+        const float* q = src.partial + (int64_t)part * 8 * src.pstride + slot;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            a[j] += (double)q[(2 * j) * src.pstride] + (double)q[(2 * j + 1) * src.pstride];
+    }
+    if (ACC) {
+        tg.ax[p] = a[0] * G;
+        tg.ay[p] = a[1] * G;
+        tg.az[p] = a[2] * G;
+    }
+    if (POT) {
+        double phi = -a[3];
+        if (LAW == NB_LAW_PLUMMER && tg.self_mass) {
+            const float h = (float)(tg.type ? tg.soft[tg.type[p] - 1] : tg.h_const);
+            phi += (double)((float)tg.self_mass[p] * rsqrt_approx(h * h));
+        }
+        tg.pot[p] = phi * G;
+    }
+}
+
 template <int LAW, bool ACC, bool POT>
 static cudaError_t launch_cfg(const Sources32& src, const Targets& tg, double G, uint32_t* err,
                               int block, int ipt, cudaStream_t s) {
     const int64_t per = (int64_t)block * ipt;
-    const int64_t grid = (tg.n + per - 1) / per;
+    const int js = src.jsplit > 1 ? src.jsplit : 1;
+    const int64_t grid = (tg.n + per - 1) / per * js;
     if (grid <= 0) return cudaSuccess;
+    if (js > 1) {
+        cudaError_t e = cudaSuccess;
+#define NB_LAUNCH_J(B, I)                                                            \
+        if (block == B && ipt == I)                                                 \
+            k_force_mixed<LAW, ACC, POT, B, I><<<(unsigned)grid, B, 0, s>>>(src, tg, G, err);
+        NB_LAUNCH_J(128, 1)
+        else NB_LAUNCH_J(128, 2) else NB_LAUNCH_J(128, 4) else NB_LAUNCH_J(256, 1)
+        else NB_LAUNCH_J(256, 2) else NB_LAUNCH_J(256, 4) else return cudaErrorInvalidValue;
+#undef NB_LAUNCH_J
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_force_join<LAW, ACC, POT><<<(unsigned)((tg.n + 255) / 256), 256, 0, s>>>(src, tg, G);
+        return cudaGetLastError();
+    }
 #define NB_LAUNCH(B, I)                                                           \
     if (block == B && ipt == I) {                                                 \
         k_force_mixed<LAW, ACC, POT, B, I><<<(unsigned)grid, B, 0, s>>>(src, tg, G, err); \

@@ -187,6 +187,63 @@ cudaError_t launch_kick(double* vx, double* vy, double* vz, const double* ax, co
     return cudaGetLastError();
 }
 
+// postprocessing_force (src/directsumgpu/gravity.jl:64-79; CPU
+// src/base/PostProcessing/Force.jl:33-47), for the particles that received a
+// force (Ti_endstep == t_int, or all with constant steps):
+//   background field: point mass a += -GM / (r.r) * r / |r| (the attractor of
+//     test/Local-Timestep.jl:746), or pseudo-Newtonian a += -GM / (|r| - r_g)^2
+//     * r / |r| (src/tools/BlackHole.jl:41-60), r = x - centre;
+//   then Milgrom (1983): a *= nu(|a| / ACC0, n),
+//     nu(y, n) = (0.5 (1 + sqrt(1 + 4 y^-n)))^(1/n) (src/mond/milgrom1983.jl:6-8, 36-51).
+// A particle with a = 0 keeps a = 0 under MOND (the limit of a nu(a)); the
+// reference's expression gives 0 * Inf = NaN there.
+__global__ void k_postprocess(double* __restrict__ ax, double* __restrict__ ay,
+                              double* __restrict__ az, const double* __restrict__ x,
+                              const double* __restrict__ y, const double* __restrict__ z,
+                              const int64_t* __restrict__ ti_end, int64_t n, const Clock* clk,
+                              int active_only, PostCfg c) {
+    const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n) return;
+    if (active_only && ti_end[i] != clk->t_int) return;
+    double a0 = ax[i], a1 = ay[i], a2 = az[i];
+    if (c.bg_kind != NB_BG_NONE) {
+        const double rx = x[i] - c.cx, ry = y[i] - c.cy, rz = z[i] - c.cz;
+        const double r2 = rx * rx + ry * ry + rz * rz;
+        const double r = sqrt(r2);
+        double f;
+        if (c.bg_kind == NB_BG_POINT_MASS) {
+            f = -c.gm / r2;
+        } else {
+            const double d = r - c.rg;
+            f = -c.gm / (d * d);
+        }
+        a0 = a0 + f * (rx / r);
+        a1 = a1 + f * (ry / r);
+        a2 = a2 + f * (rz / r);
+    }
+    if (c.mond == NB_MOND_MILGROM1983) {
+        const double an = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+        if (an > 0.0) {
+            const double yy = an / c.acc0;
+            const double nu = pow(0.5 * (1.0 + sqrt(1.0 + 4.0 * pow(yy, -c.nu_index))), 1.0 / c.nu_index);
+            a0 = a0 * nu;
+            a1 = a1 * nu;
+            a2 = a2 * nu;
+        }
+    }
+    ax[i] = a0;
+    ay[i] = a1;
+    az[i] = a2;
+}
+
+cudaError_t launch_postprocess(double* ax, double* ay, double* az, const double* x, const double* y,
+                               const double* z, const int64_t* ti_end, int64_t n, const Clock* clk,
+                               int active_only, PostCfg c, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_postprocess<<<grid_for(n), kBlock, 0, s>>>(ax, ay, az, x, y, z, ti_end, n, clk, active_only, c);
+    return cudaGetLastError();
+}
+
 // src/base/Timestep.jl:135-144 -- min over Ti_endstep and TimeBase.
 __global__ void k_min_reset(Clock* clk, int64_t time_base) { clk->min_endstep = time_base; }
 
@@ -258,12 +315,15 @@ cudaError_t launch_drift(double* x, double* y, double* z, const double* vx, cons
     return cudaGetLastError();
 }
 
-__global__ void k_clock_end_step(Clock* clk, int adaptive) {
+__global__ void k_clock_end_step(Clock* clk, int adaptive, int64_t n) {
     if (!adaptive) clk->last_t_float = clk->t_float;  // src/run.jl:164
+    const double targets = adaptive ? (double)clk->n_active : (double)n;
+    clk->interactions += targets * (double)n;
+    clk->steps += 1;
 }
 
-cudaError_t launch_clock_end_step(Clock* clk, int adaptive, cudaStream_t s) {
-    k_clock_end_step<<<1, 1, 0, s>>>(clk, adaptive);
+cudaError_t launch_clock_end_step(Clock* clk, int adaptive, int64_t n, cudaStream_t s) {
+    k_clock_end_step<<<1, 1, 0, s>>>(clk, adaptive, n);
     return cudaGetLastError();
 }
 

@@ -35,6 +35,8 @@ struct Clock {
     double dt_drift;        // interval of the pending drift
     int32_t n_active;       // active particles at t_int
     uint32_t err;           // DEVERR_* bits
+    double interactions;    // sum over steps of (targets x sources)
+    int64_t steps;          // steps taken through the step graph
 };
 
 // Timestep configuration passed by value.
@@ -81,6 +83,13 @@ struct Sources32 {
     const dvec4* origin;
     int32_t ntiles;
     int32_t tile_j;
+    // j-split: each i-block's tiles are shared by jsplit CTAs, which write
+    // compensated partials (partial[(part * 8 + q) * pstride + slot]) that
+    // k_force_join adds in part order.  jsplit 1: no partials.
+    int32_t jsplit;
+    int32_t pad;
+    float* partial;
+    int64_t pstride;
 };
 
 // FP64 sources.
@@ -226,6 +235,20 @@ cudaError_t launch_half_kick(double* vx, double* vy, double* vz, const double* a
                              const double* ay, const double* az, const int64_t* ti_beg,
                              const int64_t* ti_end, int64_t n, TimeCfg cfg, int forward,
                              cudaStream_t s);
+// Force post-processing (background field, then Milgrom MOND); see nb_params.
+struct PostCfg {
+    int32_t bg_kind;
+    int32_t mond;
+    double gm;
+    double cx, cy, cz;
+    double rg;
+    double acc0;
+    double nu_index;
+};
+cudaError_t launch_postprocess(double* ax, double* ay, double* az, const double* x, const double* y,
+                               const double* z, const int64_t* ti_end, int64_t n, const Clock* clk,
+                               int active_only, PostCfg c, cudaStream_t s);
+
 cudaError_t launch_kick(double* vx, double* vy, double* vz, const double* ax, const double* ay,
                         const double* az, const int32_t* type, int64_t* ti_beg, int64_t* ti_end,
                         int64_t n, TimeCfg cfg, Clock* clk, cudaStream_t s);
@@ -236,7 +259,7 @@ cudaError_t launch_min_endstep(const int64_t* ti_end, int64_t n, int64_t time_ba
 cudaError_t launch_drift(double* x, double* y, double* z, const double* vx, const double* vy,
                          const double* vz, int64_t n, TimeCfg cfg, Clock* clk, int mode,
                          int64_t t_int_arg, double t_float_arg, cudaStream_t s);
-cudaError_t launch_clock_end_step(Clock* clk, int adaptive, cudaStream_t s);
+cudaError_t launch_clock_end_step(Clock* clk, int adaptive, int64_t n, cudaStream_t s);
 cudaError_t launch_diag(const double* x, const double* y, const double* z, const double* vx,
                         const double* vy, const double* vz, const double* m, const double* pot,
                         int64_t n, double* scratch, int64_t scratch_blocks, double* out8,

@@ -46,6 +46,15 @@ struct NbParams
     tile_j::Int32
     i_per_thread::Int32
     block::Int32
+    j_split::Int32
+    reserved::Int32
+    bg_kind::Int32
+    mond::Int32
+    bg_gm::Float64
+    bg_center::NTuple{3,Float64}
+    bg_rg::Float64
+    mond_acc0::Float64
+    mond_nu_index::Float64
 end
 
 struct NbDiag
@@ -76,6 +85,11 @@ timeunit(sim) = isnothing(sim.config.units) ? nothing : sim.config.units[2]
 strip(u, x) = isnothing(u) ? Float64(x) : Float64(ustrip(u, x))
 stripG(sim) = Float64(ustrip(sim.config.constants.G))
 
+accunit(sim) = isnothing(sim.config.units) ? nothing : sim.config.units[1] / sim.config.units[2]^2
+mond_of(sim) = Int32(sim.config.grav.model isa AstroNbodySim.MOND1983Milgrom ? 1 : 0)
+
+# Background-force closures (sim.bgforce) cannot cross the C ABI: analytic fields
+# are selected through bg_kind / bg_gm / bg_center / bg_rg of NbParams instead.
 function params(sim; precision = Int32(1), law = Int32(0))
     tc = sim.config.time
     step = tc.step
@@ -88,7 +102,11 @@ function params(sim; precision = Int32(1), law = Int32(0))
              adaptive ? strip(tu, step.MinStep) : 1.0e-8,
              adaptive ? strip(tu, step.MaxStep) : Inf,
              adaptive ? Int64(step.TimeBase) : Int64(1) << 30,
-             strip(tu, tc.Begin), strip(tu, tc.End), Int32(0), Int32(0), Int32(0), Int32(0))
+             strip(tu, tc.Begin), strip(tu, tc.End), Int32(0), Int32(0), Int32(0), Int32(0),
+             Int32(0), Int32(0),
+             Int32(0), mond_of(sim), 0.0, (0.0, 0.0, 0.0), 0.0,
+             mond_of(sim) == 0 ? 0.0 : strip(accunit(sim), sim.config.constants.ACC0),
+             Float64(sim.config.grav.MOND_nuIndex))
 end
 
 """Create the library handle for `sim` and upload its particles (replaces the
@@ -185,6 +203,29 @@ end
 
 # src/directsum/potential.jl:150-153 and src/base/Energy.jl (GPU versions)
 AstroNbodySim.total_potential(sim::Simulation, ::DirectSum, ::GPU) = diag(sim, 1).potential
+
+# src/restart.jl:14-19: the (DirectSum, GPU) restart file holds the device image
+function AstroNbodySim.saverestart(sim::Simulation, ::DirectSum, ::GPU)
+    routed(sim) || return invoke(AstroNbodySim.saverestart, Tuple{Simulation,DirectSum,GPU}, sim, DirectSum(), GPU())
+    h = handle(sim)
+    nbytes = Ref{Int64}(0)
+    check(h, ccall((:nb_checkpoint_size, libnb), Cint, (Ptr{Cvoid}, Ref{Int64}), h.ptr, nbytes))
+    buf = Vector{UInt8}(undef, nbytes[])
+    GC.@preserve buf check(h, ccall((:nb_checkpoint_save, libnb), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int64),
+                                    h.ptr, buf, nbytes[]))
+    write(joinpath(sim.config.output.dir, "restart.$(AstroNbodySim.Distributed.myid()).nbgb300"), buf)
+    return nothing
+end
+
+"""Load a device image written by `saverestart` into the handle of `sim`
+(a Simulation built with the same configuration), replacing its state."""
+function loadrestart!(sim::Simulation, filename::AbstractString)
+    h = handle(sim)
+    buf = read(filename)
+    GC.@preserve buf check(h, ccall((:nb_checkpoint_load, libnb), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int64),
+                                    h.ptr, buf, length(buf)))
+    return sim
+end
 
 """Copy the resident state back into `sim.simdata` (units re-attached by the
 caller's StructArray element types); replaces get_all_data for GPU

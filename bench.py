@@ -175,7 +175,9 @@ def run_gpu(args):
     data = nb.plummer(n, seed=2 + rank)
     sim = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
                         precision="mixed", law=args.law, device=local, block=args.block,
-                        i_per_thread=args.ipt)
+                        i_per_thread=args.ipt, j_split=args.jsplit,
+                        tuning=None if (args.block or args.ipt or args.jsplit) else "auto")
+    tuned = sim.tuned_shape
     stream = torch.cuda.Stream(device=dev)
     sim.set_stream(stream.cuda_stream)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
@@ -215,6 +217,7 @@ def run_gpu(args):
 
     # ---- resident run: warm-up, then K timed steps ------------------------
     nb.run  # noqa: B018  (API reference for readers)
+    d0 = nb.diagnostics(sim) if rank == 0 and not args.skip_accuracy else None
     sim._ck(sim._lib.nb_run_begin(sim.handle))
     for _ in range(args.warmup):
         nb.step(sim, 1)
@@ -257,6 +260,16 @@ def run_gpu(args):
     clocks = sampler.stop()
     force_ms = statistics.mean(a.elapsed_time(b) for a, b in fev)
 
+    # ---- energy drift of the run: synchronised state (virtual back half kick)
+    if d0 is not None:
+        nb.leapfrog_half_kick(sim, -1)
+        d1 = nb.diagnostics(sim)
+        e0, e1 = d0["K"] + d0["W"], d1["K"] + d1["W"]
+        acc_stats["energy_drift_mixed_n%d" % n] = {
+            "steps": args.warmup + args.steps, "dt": DT, "energy_rel_drift": (e1 - e0) / abs(e0),
+            "momentum_abs_drift": float(np.linalg.norm(d1["P"] - d0["P"]))}
+        acc_stats["energy_drift_mixed_vs_fp64_n32768"] = energy_drift_pair(nb, args.law, local)
+
     # ---- end to end through the public API with host buffers ---------------
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
            for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "m")}
@@ -286,27 +299,7 @@ def run_gpu(args):
     sim.close()
 
     # ---- batched ensemble (many independent systems, one engine) -----------
-    batch = None
-    if not args.skip_batch:
-        ens = nb.ensemble_systems(args.batch_systems, seed=11 + rank)
-        tot = sum(d["pos"].shape[0] for d, _ in ens)
-        eng = nb.Engine(max_particles=tot + 4096, max_systems=args.batch_systems,
-                        max_steps_per_call=args.batch_steps, device=local, law=args.law)
-        for d, eps in ens:
-            eng.submit(d, eps, 1e-3, args.batch_steps)
-        del ens
-        t0 = time.perf_counter()
-        eng.run_until_idle()
-        t_batch_wall = time.perf_counter() - t0
-        st = eng.stats()
-        eng.close()
-        batch = {"value": st["interactions"] / (st["gpu_ms"] / 1e3) / 1e9, "unit": UNIT,
-                 "systems": args.batch_systems, "particles": tot, "steps": args.batch_steps,
-                 "interactions": st["interactions"], "gpu_s": st["gpu_ms"] / 1e3,
-                 "wall_s_incl_admission_and_retirement": t_batch_wall,
-                 "workload": "N log-uniform [64, 8192], half Plummer / half Hernquist (a=1, r<100a), "
-                             "m=1/N, eps U[1e-3, 1e-2], mixed, %d KDK steps dt=1e-3, one CUDA graph "
-                             "per step" % args.batch_steps}
+    batch = None if args.skip_batch else run_ensemble(nb, args, rank, local)
 
     # ---- serving sample (Poisson arrivals, continuous batching) ------------
     serve_stats = None
@@ -361,9 +354,11 @@ def run_gpu(args):
                        "step": "drift+pack+force(N^2)+kick, one CUDA graph replay",
                        "l2": "256 MiB write between timed steps, outside the events",
                        "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "force_kernel": ("auto: direct grid 128 threads x 1 target for N >= 2^19, "
-                                        "persistent work list below" if not (args.block or args.ipt)
-                                        else "block=%d i_per_thread=%d" % (args.block, args.ipt))},
+                       "force_kernel": ("block=%d i_per_thread=%d j_split=%d (%s)" % (
+                           tuned[0], tuned[1], tuned[2],
+                           "explicit" if (args.block or args.ipt or args.jsplit) else
+                           ("autotuner table" if tuned[:2] != (0, 0) else
+                            "built-in rule: direct 128x1 for N >= 2^19, work list below")))},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak_tflops,
                          "unit": "TFLOP/s", "frac": achieved / fp32_peak_tflops, "traffic": traffic,
                          "kernel": "k_force_mixed (+k_pack)", "force_ms": force_ms,
@@ -382,6 +377,99 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def run_ensemble(nb, args, rank=0, local=0):
+    """Batched ensemble: args.batch_systems systems through one engine for
+    args.batch_steps KDK steps; aggregate interactions/s over the engine's
+    CUDA-event time."""
+    ens = nb.ensemble_systems(args.batch_systems, seed=11 + rank)
+    tot = sum(d["pos"].shape[0] for d, _ in ens)
+    eng = nb.Engine(max_particles=tot + 4096, max_systems=args.batch_systems,
+                    max_steps_per_call=args.batch_steps, device=local, law=args.law)
+    for d, eps in ens:
+        eng.submit(d, eps, 1e-3, args.batch_steps)
+    del ens
+    t0 = time.perf_counter()
+    eng.run_until_idle()
+    t_batch_wall = time.perf_counter() - t0
+    st = eng.stats()
+    eng.close()
+    return {"value": st["interactions"] / (st["gpu_ms"] / 1e3) / 1e9, "unit": UNIT,
+            "systems": args.batch_systems, "particles": tot, "steps": args.batch_steps,
+            "interactions": st["interactions"], "gpu_s": st["gpu_ms"] / 1e3,
+            "wall_s_incl_admission_and_retirement": t_batch_wall,
+            "workload": "N log-uniform [64, 8192], half Plummer / half Hernquist (a=1, r<100a), "
+                        "m=1/N, eps U[1e-3, 1e-2], mixed, %d KDK steps dt=1e-3, one CUDA graph "
+                        "per step" % args.batch_steps}
+
+
+def energy_drift_pair(nb, law, device, n=32768, steps=10):
+    """Energy / momentum drift of `steps` KDK steps at dt 1e-4 of a Plummer
+    sphere (eps 1e-3), mixed and plain FP64 on the GPU from the same state."""
+    data = nb.plummer(n, seed=99)
+    out = {"n": n, "steps": steps, "dt": DT}
+    for prec in ("mixed", "fp64"):
+        sim = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
+                            precision=prec, law=law, device=device)
+        d0 = nb.diagnostics(sim)
+        nb.run(sim, nsteps=steps)
+        d1 = nb.diagnostics(sim)
+        e0, e1 = d0["K"] + d0["W"], d1["K"] + d1["W"]
+        out[prec] = {"energy_rel_drift": (e1 - e0) / abs(e0),
+                     "momentum_abs_drift": float(np.linalg.norm(d1["P"] - d0["P"]))}
+        if prec == "mixed":
+            pos_m = nb.get_all_data(sim)["pos"]
+        else:
+            out["final_pos_max_abs_diff"] = float(np.abs(nb.get_all_data(sim)["pos"] - pos_m).max())
+        sim.close()
+    return out
+
+
+def run_collision(args):
+    """Two Hernquist spheres on a parabolic approach, adaptive power-of-two bins
+    with dt_i = eta sqrt(eps / |a_i|) (eta 0.025, dt_max 1e-2), eps 5e-3.
+    Throughput of the mixed adaptive run over `--base-steps` base steps of
+    dt_max; with --fp64-compare also an FP64 GPU run of the same initial
+    conditions (energy / momentum drift of both)."""
+    import torch
+
+    import astronbodysim as nb
+
+    n_each = args.n_each
+    data = nb.collision(n_each, seed=5, separation=20.0)
+    T = args.base_steps * 1e-2
+    out = {"mode": "collision", "n": 2 * n_each, "base_steps": args.base_steps, "eps": 5e-3,
+           "criterion": "eta_sqrt_eps", "eta": 0.025, "dt_max": 1e-2, "unit": UNIT}
+    for prec in (["mixed", "fp64"] if args.fp64_compare else ["mixed"]):
+        sim = nb.Simulation(data, ForceSofteningTable=[5e-3] * 6, TimeEnd=T, MaxStep=1e-2,
+                            ErrTolTimestep=0.025, criterion="eta_sqrt_eps", precision=prec,
+                            tuning="auto" if prec == "mixed" else None)
+        d0 = nb.diagnostics(sim)
+        nb.compute_force(sim)
+        nb.init_timesteps(sim)
+        nb.leapfrog_half_kick(sim, +1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        while True:
+            nb.step(sim, 1)
+            _, tf = sim.time()
+            if tf >= T:
+                break
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        substeps, pairs = nb.counters(sim)
+        nb.leapfrog_half_kick(sim, -1)
+        d1 = nb.diagnostics(sim)
+        e0, e1 = d0["K"] + d0["W"], d1["K"] + d1["W"]
+        out[prec] = {"substeps": substeps, "wall_s": wall, "interactions": pairs,
+                     "g_interactions_per_s": pairs / wall / 1e9,
+                     "energy_rel_drift": (e1 - e0) / abs(e0),
+                     "momentum_abs_drift": float(np.linalg.norm(d1["P"] - d0["P"])),
+                     "angular_momentum_abs_drift": float(np.linalg.norm(d1["L"] - d0["L"]))}
+        sim.close()
+    print(json.dumps(out), flush=True)
     return 0
 
 
@@ -412,6 +500,7 @@ def main():
     ap.add_argument("--law", default="spline", choices=["spline", "plummer"])
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--ipt", type=int, default=0)
+    ap.add_argument("--jsplit", type=int, default=0)
     ap.add_argument("--force-reps", type=int, default=3)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--acc-targets", type=int, default=4096)
@@ -426,12 +515,31 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-particles", type=int, default=1 << 22)
-    ap.add_argument("--mode", default="bench", choices=["bench", "serve"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "serve", "collision", "tune", "ensemble"])
+    ap.add_argument("--n-each", type=int, default=1 << 20)
+    ap.add_argument("--base-steps", type=int, default=2)
+    ap.add_argument("--fp64-compare", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.mode == "serve":
         return run_serve(args)
+    if args.mode == "collision":
+        return run_collision(args)
+    if args.mode == "ensemble":
+        import astronbodysim as nb
+
+        out = run_ensemble(nb, args)
+        out["mode"] = "ensemble"
+        print(json.dumps(out), flush=True)
+        return 0
+    if args.mode == "tune":
+        from astronbodysim import autotune
+
+        for law in ("spline", "plummer"):
+            autotune.save(autotune.tune([1 << k for k in range(12, 21)], law=law, reps=3))
+        print(json.dumps(autotune.load()), flush=True)
+        return 0
     return run_gpu(args)
 
 

@@ -68,7 +68,31 @@ typedef struct nb_params {
     int32_t i_per_thread; /* tuning override (0 = auto) */
     int32_t block;        /* tuning override: threads per CTA of the direct grid (128, 256);
                              -1 = persistent work-list kernel; 0 (with i_per_thread 0) = auto */
+    int32_t j_split;      /* tuning override: CTAs sharing one i-block's sources in the direct
+                             grid (1..4; 0 = 1) */
+    int32_t reserved;
+    /* Force post-processing, applied by nb_compute_force and nb_step to the
+     * particles that received a force (postprocessing_force,
+     * src/directsumgpu/gravity.jl:64-79; CPU src/base/PostProcessing/Force.jl:33-47):
+     * first an analytic background field (the reference's bgforce closures,
+     * as the point-mass attractor of test/Local-Timestep.jl:746 or the
+     * pseudo-Newtonian field of src/tools/BlackHole.jl:41-60), then the
+     * Milgrom (1983) MOND correction a *= nu(|a| / ACC0, MOND_nuIndex)
+     * (src/mond/milgrom1983.jl:6-8, 36-51). */
+    int32_t bg_kind;      /* NB_BG_NONE, NB_BG_POINT_MASS, NB_BG_PSEUDO_NEWTONIAN */
+    int32_t mond;         /* NB_MOND_NONE, NB_MOND_MILGROM1983 */
+    double bg_gm;         /* G * M of the central object */
+    double bg_center[3];  /* its position */
+    double bg_rg;         /* gravity radius r_g of NB_BG_PSEUDO_NEWTONIAN */
+    double mond_acc0;     /* ACC0 (> 0 when mond is set) */
+    double mond_nu_index; /* MOND_nuIndex (reference default 2) */
 } nb_params;
+
+#define NB_BG_NONE 0
+#define NB_BG_POINT_MASS 1
+#define NB_BG_PSEUDO_NEWTONIAN 2
+#define NB_MOND_NONE 0
+#define NB_MOND_MILGROM1983 1
 
 /* Energy / momentum diagnostics, FP64 (src/base/Energy.jl:13-101). */
 typedef struct nb_diag {
@@ -172,8 +196,26 @@ int nb_get_time(nb_handle *h, int64_t *t_int, double *t_float);
  * (src/base/Energy.jl:13-101, src/directsum/potential.jl:150-153). */
 int nb_diagnostics(nb_handle *h, int with_potential, nb_diag *out);
 
+/* Steps taken by nb_step since the upload, and the pair evaluations they made
+ * (active targets x all sources per step). */
+int nb_get_counters(nb_handle *h, int64_t *steps, double *interactions);
+
 /* Number of particles active at the current time (Ti_endstep == t_int). */
 int nb_active_count(nb_handle *h, int64_t *count);
+
+/* Device-state checkpoint, replacing saverestart for (DirectSum, GPU)
+ * (src/restart.jl:14-19) and loadrestart (src/restart.jl:129-139).  The image
+ * is one host buffer: parameters, particles (x, v, a, pot, m, type,
+ * Ti_begstep, Ti_endstep) and the device time line.  nb_checkpoint_size gives
+ * its size for the current particle count; nb_checkpoint_save fills a buffer
+ * of at least that size; nb_checkpoint_load replaces the state and parameters
+ * of a handle (of any size, on its own device) with an image, after which the
+ * run continues bit-identically to the saved one.  Images are checked for the
+ * magic, version and sizes of this library and rejected with
+ * NB_ERR_INVALID_ARG otherwise. */
+int nb_checkpoint_size(nb_handle *h, int64_t *bytes);
+int nb_checkpoint_save(nb_handle *h, void *buf, int64_t bytes);
+int nb_checkpoint_load(nb_handle *h, const void *buf, int64_t bytes);
 
 /* Mixed-precision acceleration (and, if pot != NULL, potential per unit mass)
  * of n particles from the same n particles, one softening length for all,
@@ -221,6 +263,7 @@ typedef struct nb_engine_params {
 #define NB_REQ_RUNNING 1
 #define NB_REQ_DONE 2
 #define NB_REQ_CANCELLED 3
+#define NB_REQ_SUSPENDED 4
 
 typedef struct nb_engine_stats {
     int64_t queued;
@@ -249,6 +292,15 @@ int nb_batch_poll(nb_engine *e, int64_t id, int32_t *state, int64_t *steps_done)
 int nb_batch_fetch(nb_engine *e, int64_t id, double *x, double *y, double *z, double *vx,
                    double *vy, double *vz);
 int nb_batch_cancel(nb_engine *e, int64_t id);
+/* Evict a running system to host memory (positions, half-step velocities,
+ * accelerations, masses, its Morton order and step count), freeing its arena
+ * range and slot; state NB_REQ_SUSPENDED.  nb_batch_resume queues it again
+ * (FIFO); once re-admitted it continues without a new start-up force or half
+ * kick, and its result is bit-identical to an uninterrupted run.  The
+ * reference has no batch engine; this is the per-request form of its restart
+ * files (src/restart.jl). */
+int nb_batch_suspend(nb_engine *e, int64_t id);
+int nb_batch_resume(nb_engine *e, int64_t id);
 int nb_engine_get_stats(nb_engine *e, nb_engine_stats *out);
 /* Ids of systems finished since the previous call (up to cap; *count set). */
 int nb_engine_drain_done(nb_engine *e, int64_t *ids, int64_t cap, int64_t *count);

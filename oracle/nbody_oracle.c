@@ -251,6 +251,11 @@ typedef struct or_state {
     double t_float, last_t_float;
     int32_t mode; /* summation mode for forces */
     int32_t pad;
+    /* force post-processing (src/base/PostProcessing/Force.jl:33-47) */
+    int32_t bg_kind; /* 0 none, 1 point mass, 2 pseudo-Newtonian */
+    int32_t mond;    /* 0 Newton, 1 Milgrom (1983) */
+    double bg_gm, bg_cx, bg_cy, bg_cz, bg_rg;
+    double mond_acc0, mond_nu_index;
 } or_state;
 
 static inline double soft_of(const or_state *s, int64_t i) { return s->soft[s->type[i] - 1]; }
@@ -275,7 +280,51 @@ static int get_timestep(const or_state *s, double ax, double ay, double az, doub
     return OR_OK;
 }
 
-/* Force on active particles: gravity.jl:80-101 (active = Ti_endstep == now). */
+/* postprocessing_force for the CPU (src/base/PostProcessing/Force.jl:33-47):
+ * background field of the active particles (bgforce closures; the point-mass
+ * attractor of test/Local-Timestep.jl:746, the pseudo-Newtonian field of
+ * src/tools/BlackHole.jl:41-60), then Milgrom (1983) MOND
+ * (src/mond/milgrom1983.jl:6-8, 36-51).  a = 0 stays 0 under MOND. */
+static void postprocess(or_state *s, const uint8_t *act)
+{
+    if (s->bg_kind == 0 && s->mond == 0) return;
+    for (int64_t i = 0; i < s->n; ++i) {
+        if (!act[i]) continue;
+        double a0 = s->ax[i], a1 = s->ay[i], a2 = s->az[i];
+        if (s->bg_kind != 0) {
+            double rx = s->x[i] - s->bg_cx, ry = s->y[i] - s->bg_cy, rz = s->z[i] - s->bg_cz;
+            double r2 = rx * rx + ry * ry + rz * rz;
+            double r = sqrt(r2);
+            double f;
+            if (s->bg_kind == 1) {
+                f = -s->bg_gm / r2;
+            } else {
+                double d = r - s->bg_rg;
+                f = -s->bg_gm / (d * d);
+            }
+            a0 = a0 + f * (rx / r);
+            a1 = a1 + f * (ry / r);
+            a2 = a2 + f * (rz / r);
+        }
+        if (s->mond == 1) {
+            double an = sqrt(a0 * a0 + a1 * a1 + a2 * a2);
+            if (an > 0.0) {
+                double y = an / s->mond_acc0;
+                double nu = pow(0.5 * (1.0 + sqrt(1.0 + 4.0 * pow(y, -s->mond_nu_index))),
+                                1.0 / s->mond_nu_index);
+                a0 = a0 * nu;
+                a1 = a1 * nu;
+                a2 = a2 * nu;
+            }
+        }
+        s->ax[i] = a0;
+        s->ay[i] = a1;
+        s->az[i] = a2;
+    }
+}
+
+/* Force on active particles: gravity.jl:80-101 (active = Ti_endstep == now),
+ * then the post-processing above. */
 int or_compute_force(or_state *s, int want_pot)
 {
     int64_t n = s->n;
@@ -292,6 +341,7 @@ int or_compute_force(or_state *s, int want_pot)
     }
     int rc = or_force(n, s->x, s->y, s->z, s->m, n, s->x, s->y, s->z, th, act, s->G, s->law,
                       s->mode, s->ax, s->ay, s->az, want_pot ? s->pot : NULL, s->nthreads);
+    if (rc == OR_OK) postprocess(s, act);
     free(th);
     free(act);
     return rc;

@@ -52,6 +52,15 @@ class _State(ctypes.Structure):
         ("last_t_float", ctypes.c_double),
         ("mode", ctypes.c_int32),
         ("pad", ctypes.c_int32),
+        ("bg_kind", ctypes.c_int32),
+        ("mond", ctypes.c_int32),
+        ("bg_gm", ctypes.c_double),
+        ("bg_cx", ctypes.c_double),
+        ("bg_cy", ctypes.c_double),
+        ("bg_cz", ctypes.c_double),
+        ("bg_rg", ctypes.c_double),
+        ("mond_acc0", ctypes.c_double),
+        ("mond_nu_index", ctypes.c_double),
     ]
 
 
@@ -155,7 +164,9 @@ class OracleSim:
 
     def __init__(self, pos, vel, mass, ptype=None, soft=(1e-4,) * 6, G=1.0, law=LAW_SPLINE_G2,
                  dt=None, eta=0.025, min_step=1e-8, max_step=float("inf"), time_base=1 << 30,
-                 time_begin=0.0, time_end=0.1, criterion=CRIT_REF, mode=0, nthreads=0):
+                 time_begin=0.0, time_end=0.1, criterion=CRIT_REF, mode=0, nthreads=0,
+                 bg_kind=0, bg_gm=0.0, bg_center=(0.0, 0.0, 0.0), bg_rg=0.0, mond=0,
+                 mond_acc0=0.0, mond_nu_index=2.0):
         pos = _f64(pos).reshape(-1, 3)
         vel = _f64(vel).reshape(-1, 3)
         n = pos.shape[0]
@@ -193,6 +204,13 @@ class OracleSim:
         s.t_float = time_begin
         s.last_t_float = time_begin
         s.mode = mode
+        s.bg_kind = bg_kind
+        s.bg_gm = bg_gm
+        s.bg_cx, s.bg_cy, s.bg_cz = (float(c) for c in bg_center)
+        s.bg_rg = bg_rg
+        s.mond = mond
+        s.mond_acc0 = mond_acc0
+        s.mond_nu_index = mond_nu_index
         self._s = s
 
     def _call(self, name, *args):

@@ -110,3 +110,52 @@ def test_engine_errors_and_cancel(nb):
     assert eng.poll(r1)[0] == nb._lib.NB_REQ_DONE
     with pytest.raises(nb.NbodyError):
         eng.poll(999999)
+
+
+@pytest.mark.parametrize("n", [2000, 20000])
+@pytest.mark.parametrize("at", [21, 32])
+def test_suspend_resume_is_bit_identical(nb, n, at):
+    """A system evicted to the host after `at` steps (mid re-ordering period,
+    and on a re-ordering step), kept out while others run, then resumed,
+    ends bit-identical to the uninterrupted run.  n = 20000 is ordered by the
+    global radix sort, n = 2000 in shared memory."""
+    target = nb.plummer(n, seed=61)
+    others = systems(nb, [700, 3000], seed=62)
+    dt, nsteps = 1e-3, 60
+
+    ref_eng = nb.Engine(max_particles=1 << 16, max_systems=8, max_steps_per_call=8)
+    rid = ref_eng.submit(target, 0.01, dt, nsteps)
+    ref_eng.run_until_idle()
+    ref = ref_eng.fetch(rid, n)
+
+    eng = nb.Engine(max_particles=1 << 16, max_systems=8, max_steps_per_call=at)
+    tid = eng.submit(target, 0.01, dt, nsteps)
+    oids = [eng.submit(d, 0.005, dt, 100) for d in others]
+    eng.run()  # admits all, advances `at` steps
+    assert eng.poll(tid) == (nb._lib.NB_REQ_RUNNING, at)
+    eng.suspend(tid)
+    assert eng.poll(tid)[0] == nb._lib.NB_REQ_SUSPENDED
+    assert eng.stats()["running"] == 2
+    eng.run(5)  # the others move on
+    eng.resume(tid)
+    eng.run_until_idle()
+    got = eng.fetch(tid, n)
+    np.testing.assert_array_equal(got["pos"], ref["pos"])
+    np.testing.assert_array_equal(got["vel"], ref["vel"])
+    for rid_, d in zip(oids, others):
+        assert eng.poll(rid_)[0] == nb._lib.NB_REQ_DONE
+
+
+def test_suspend_errors(nb):
+    eng = nb.Engine(max_particles=1 << 14, max_systems=4)
+    rid = eng.submit(nb.plummer(500, seed=63), 0.01, 1e-3, 10)
+    with pytest.raises(nb.NbodyError):
+        eng.suspend(rid)  # queued, not running
+    with pytest.raises(nb.NbodyError):
+        eng.resume(rid)  # not suspended
+    eng.run(3)
+    eng.suspend(rid)
+    with pytest.raises(nb.NbodyError):
+        eng.fetch(rid, 500)  # not finished
+    eng.cancel(rid)
+    assert eng.poll(rid)[0] == nb._lib.NB_REQ_CANCELLED

@@ -195,3 +195,31 @@ def test_step_graph_matches_single_calls(nb):
     ga, gb = nb.get_all_data(a), nb.get_all_data(b)
     np.testing.assert_array_equal(ga["pos"], gb["pos"])
     np.testing.assert_array_equal(ga["vel"], gb["vel"])
+
+
+def test_collision_adaptive_mixed_vs_fp64(nb):
+    """Two Hernquist spheres on a parabolic approach, power-of-two bins from
+    dt_i = eta sqrt(eps/|a_i|) (eta 0.025, dt_max 1e-2), eps 5e-3: the mixed
+    form's energy and momentum drift stay at the FP64 run's level, and both
+    runs keep the same integer time line."""
+    data = nb.collision(1024, seed=5, separation=20.0)
+    T = 20 * 1e-2
+    res = {}
+    for prec in ("fp64", "mixed"):
+        sim = nb.Simulation(data, ForceSofteningTable=[5e-3] * 6, TimeEnd=T, MaxStep=1e-2,
+                            criterion="eta_sqrt_eps", precision=prec)
+        d0 = nb.diagnostics(sim)
+        nb.run(sim)
+        d1 = nb.diagnostics(sim)
+        steps, pairs = nb.counters(sim)
+        assert steps > 20 and pairs >= steps * 1.0 and pairs <= steps * 2048.0 * 2048.0
+        res[prec] = (d0, d1, steps, nb.get_all_data(sim))
+    for prec, (d0, d1, steps, g) in res.items():
+        e0, e1 = d0["K"] + d0["W"], d1["K"] + d1["W"]
+        assert abs(e1 - e0) / abs(e0) < 1e-3, (prec, (e1 - e0) / e0)
+        assert np.linalg.norm(d1["P"] - d0["P"]) < 1e-6
+    (f0, f1, fs, fg), (m0, m1, ms, mg) = res["fp64"], res["mixed"]
+    ef = (f1["K"] + f1["W"]) / (f0["K"] + f0["W"]) - 1
+    em = (m1["K"] + m1["W"]) / (m0["K"] + m0["W"]) - 1
+    assert abs(em - ef) < 1e-5, (em, ef)
+    np.testing.assert_allclose(mg["pos"], fg["pos"], rtol=0, atol=1e-4)
