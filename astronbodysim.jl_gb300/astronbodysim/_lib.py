@@ -83,6 +83,8 @@ class nb_engine_params(ctypes.Structure):
         ("max_particles", ctypes.c_int64),
         ("max_systems", ctypes.c_int32),
         ("max_steps_per_call", ctypes.c_int32),
+        ("block", ctypes.c_int32),
+        ("i_per_thread", ctypes.c_int32),
     ]
 
 

@@ -76,6 +76,51 @@ def tune(sizes, law="spline", reps=3, eps=1e-3, seed=0, log=print):
     return {"law": law, "entries": entries}
 
 
+BATCH_CANDIDATES = [(128, 1), (128, 2), (256, 1), (256, 2)]
+
+
+def tune_batch(nsys=1024, steps=40, law="spline", seed=5, log=print):
+    """Batch-force shape for the many-system engine: runs an ensemble of nsys
+    systems (N log-uniform in [64, 8192], half Plummer, half Hernquist) for
+    `steps` steps with every shape and keeps the one with the highest
+    interactions per GPU second."""
+    from .engine import Engine
+    from .serve import ensemble_systems
+
+    ens = ensemble_systems(nsys, seed=seed)
+    tot = sum(d["pos"].shape[0] for d, _ in ens)
+    res = {}
+    for b, i in BATCH_CANDIDATES:
+        eng = Engine(max_particles=tot + 4096, max_systems=nsys, max_steps_per_call=steps, law=law,
+                     block=b, i_per_thread=i)
+        for d, eps in ens:
+            eng.submit(d, eps, 1e-3, steps)
+        eng.run_until_idle()
+        st = eng.stats()
+        eng.close()
+        res["%dx%d" % (b, i)] = st["interactions"] / (st["gpu_ms"] / 1e3) / 1e9
+    best = max(res, key=res.get)
+    if log:
+        log("batch best=%s (%s G interactions/s)" % (best, ", ".join("%s %.0f" % kv for kv in res.items())))
+    return {"law": law, "best": best, "g_interactions_per_s": res, "systems": nsys, "steps": steps}
+
+
+def save_batch(entry, path=DEFAULT_TABLE):
+    old = load(path) or {}
+    old.setdefault("batch", {})[entry["law"]] = entry
+    with open(path, "w") as f:
+        json.dump(old, f, indent=1, sort_keys=True)
+
+
+def lookup_batch(law="spline", path=DEFAULT_TABLE):
+    """(block, i_per_thread) of the engine's batch force, or None."""
+    t = load(path)
+    if not t or "batch" not in t or law not in t["batch"]:
+        return None
+    b, i = t["batch"][law]["best"].split("x")
+    return int(b), int(i)
+
+
 def save(table, path=DEFAULT_TABLE):
     old = load(path) or {}
     old[table["law"]] = table["entries"]
@@ -94,7 +139,7 @@ def lookup(n, law="spline", path=DEFAULT_TABLE):
     """(block, i_per_thread, j_split) of the tuned shape nearest to n in log
     space, or None."""
     t = load(path)
-    if not t or law not in t or not t[law]:
+    if not t or law not in t or not t[law] or not isinstance(t[law], list):
         return None
     e = min(t[law], key=lambda e: abs(math.log(e["n"]) - math.log(max(1, n))))
     best = e["best"]

@@ -19,7 +19,7 @@ def _f64(a):
 
 class Engine:
     def __init__(self, max_particles=1 << 24, max_systems=8192, G=1.0, law="spline", device=0,
-                 max_steps_per_call=64):
+                 max_steps_per_call=64, block=0, i_per_thread=0, tuning=None):
         self._lib = L.load()
         p = L.nb_engine_params()
         p.G = float(G)
@@ -28,6 +28,17 @@ class Engine:
         p.max_particles = int(max_particles)
         p.max_systems = int(max_systems)
         p.max_steps_per_call = int(max_steps_per_call)
+        if tuning and not block and not i_per_thread:
+            # batch-force shape from the autotuner's table
+            from . import autotune
+
+            shape = autotune.lookup_batch(law=law, path=autotune.DEFAULT_TABLE if tuning == "auto"
+                                          else tuning)
+            if shape:
+                block, i_per_thread = shape
+        p.block = int(block)
+        p.i_per_thread = int(i_per_thread)
+        self.shape = (int(block) or 128, int(i_per_thread) or 2)
         h = ctypes.c_void_p()
         rc = self._lib.nb_engine_create(ctypes.byref(p), ctypes.byref(h))
         if rc != L.NB_OK:

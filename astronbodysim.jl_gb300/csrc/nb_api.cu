@@ -36,6 +36,7 @@ struct nb_handle {
     void* sort_scratch = nullptr;
     float4* pack = nullptr;
     nb::dvec4* origin = nullptr;
+    float4* ext = nullptr;
     int32_t ntiles = 0;
     double* diag_scratch = nullptr;
     int64_t diag_blocks = 0;
@@ -203,7 +204,7 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     // coordinates relative to its origin stay small.
     e = nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, s);
     if (e != cudaSuccess) return e;
-    e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, s);
+    e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
     // Measured on GB300 (Plummer, spline): the direct grid with one target per
     // thread is fastest from N = 2^19 up; below, the evenly split work list
@@ -238,6 +239,7 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
         w.perm = active_only ? nullptr : h->perm;
         w.pack = h->pack;
         w.origin = h->origin;
+        w.ext = h->ext;
         w.x = h->x;
         w.y = h->y;
         w.z = h->z;
@@ -264,7 +266,7 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
             t2.idx = h->perm;
         }
     }
-    nb::Sources32 src{h->pack, h->origin, h->ntiles, kTileJ};
+    nb::Sources32 src{h->pack, h->origin, h->ext, h->ntiles, kTileJ};
     if (particles && h->jsplit > 1) {
         src.jsplit = h->jsplit;
         src.partial = h->jpartial;
@@ -348,6 +350,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     size_t o_sort = take(nb::sort_scratch_bytes(n));
     size_t o_pack = take(sizeof(float4) * (size_t)npad);
     size_t o_orig = take(sizeof(nb::dvec4) * (size_t)ntiles);
+    size_t o_ext = take(sizeof(float4) * (size_t)ntiles);
     size_t o_ds = take(sizeof(double) * (size_t)dblocks);
     size_t o_do = take(sizeof(double) * 8);
     void* a = nullptr;
@@ -377,6 +380,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->sort_scratch = (void*)(b + o_sort);
     h->pack = (float4*)(b + o_pack);
     h->origin = (nb::dvec4*)(b + o_orig);
+    h->ext = (float4*)(b + o_ext);
     h->diag_scratch = (double*)(b + o_ds);
     h->diag_blocks = dblocks / 8;
     h->diag_out = (double*)(b + o_do);

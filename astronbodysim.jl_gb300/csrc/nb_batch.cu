@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(kTileJ)
                  const double* __restrict__ bbox, const int32_t* __restrict__ perm,
                  const double* __restrict__ x, const double* __restrict__ y,
                  const double* __restrict__ z, const double* __restrict__ m,
-                 float4* __restrict__ pack, dvec4* __restrict__ origin) {
+                 float4* __restrict__ pack, dvec4* __restrict__ origin, float4* __restrict__ ext) {
     // The tile's bounding box is reduced in FP32 relative to the tile's first
     // particle c (FP64); the tile origin c + float offset is exact in FP64 and
     // the sources are then re-expressed relative to it in FP64.  Everything
@@ -322,6 +322,10 @@ __global__ void __launch_bounds__(kTileJ)
                                  fmaxf(fmaxf(fabsf(lo[1]), fabsf(hi[1])),
                                        fmaxf(fabsf(lo[2]), fabsf(hi[2]))));
         origin[g] = make_dvec4(ox, oy, oz, (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
+        // box half extents for the near test, enlarged the same way
+        const float slack = 4.0e-7f * amax;
+        ext[g] = make_float4(0.5f * ex * (1.0f + 1e-5f) + slack, 0.5f * ey * (1.0f + 1e-5f) + slack,
+                             0.5f * ez * (1.0f + 1e-5f) + slack, rr);
     }
 }
 
@@ -331,15 +335,14 @@ __global__ void __launch_bounds__(kTileJ)
 // the CTA streams all j-tiles of that system through the bulk-copy ring, in
 // order, exactly like the single-system kernel.
 // ---------------------------------------------------------------------------
-constexpr int kFBlock = 128;
-constexpr int kFIpt = 2;
-constexpr int kFBt = kFBlock * kFIpt;
-
-template <int LAW, bool ACC, bool POT>
-__global__ void __launch_bounds__(kFBlock, (ACC && !POT) ? 8 : 1) k_force_batch(BatchForce f) {
-    constexpr int IPT = kFIpt;
-    constexpr int BLOCK = kFBlock;
-    constexpr int NW = kFBlock / 32;
+// Launch shapes (threads per CTA, targets per thread); an item is one i-block
+// of BLOCK * IPT targets.  Default 128 x 2; the engine takes the shape from its
+// parameters (chosen by the autotuner).
+template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
+__global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) : 1)
+    k_force_batch(BatchForce f) {
+    constexpr int NW = BLOCK / 32;
+    constexpr int kFBt = BLOCK * IPT;
     __shared__ __align__(128) float4 buf[kStages * kTileJ];
     __shared__ __align__(8) uint64_t full[kStages];
     __shared__ uint32_t done[kStages];
@@ -431,16 +434,8 @@ __global__ void __launch_bounds__(kFBlock, (ACC && !POT) ? 8 : 1) k_force_batch(
             }
             const float4* b = &buf[st * kTileJ];
             bool near = false;
-            if (LAW == NB_LAW_SPLINE_G2) {
-                const float R = (float)o.w;
-#pragma unroll
-                for (int k = 0; k < IPT; ++k) {
-                    const float d2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
-                    const float lim = (R + hh[k]) * 1.0001f;
-                    near |= (pidx[k] >= 0) && (d2 <= lim * lim);
-                }
-                near = __any_sync(0xffffffffu, near);
-            }
+            if (LAW == NB_LAW_SPLINE_G2)
+                near = warp_near<IPT>(f.ext[d.tile_off + t], xr, yr, zr, hh, pidx);
             if (near)
                 pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
             else
@@ -497,45 +492,69 @@ __global__ void __launch_bounds__(kFBlock, (ACC && !POT) ? 8 : 1) k_force_batch(
     }
 }
 
-template <int LAW, bool ACC, bool POT>
-static int batch_occ() {
+bool batch_shape_ok(int block, int ipt) {
+    return (block == 128 || block == 256) && (ipt == 1 || ipt == 2);
+}
+
+int batch_block_targets(int block, int ipt) { return block * ipt; }
+
+// Dispatch over the compiled shapes: acceleration only (what the engine's step
+// needs); 128 x 2 also with the potential.
+template <int LAW, bool ACC, bool POT, int B, int I>
+static int occ_of() {
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_batch<LAW, ACC, POT>, kFBlock,
-                                                      0) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_force_batch<LAW, ACC, POT, B, I>, B, 0) !=
+        cudaSuccess)
         return 1;
     return nb < 1 ? 1 : nb;
 }
 
-int batch_ctas_per_sm(int law, bool acc, bool pot) {
-    if (law == NB_LAW_PLUMMER) {
-        if (!acc) return batch_occ<NB_LAW_PLUMMER, false, true>();
-        return pot ? batch_occ<NB_LAW_PLUMMER, true, true>() : batch_occ<NB_LAW_PLUMMER, true, false>();
-    }
-    if (!acc) return batch_occ<NB_LAW_SPLINE_G2, false, true>();
-    return pot ? batch_occ<NB_LAW_SPLINE_G2, true, true>() : batch_occ<NB_LAW_SPLINE_G2, true, false>();
-}
-
-int batch_block_targets() { return kFBt; }
-
-template <int LAW, bool ACC, bool POT>
-static cudaError_t launch_fb(const BatchForce& f, int grid, cudaStream_t s) {
+template <int LAW, bool ACC, bool POT, int B, int I>
+static cudaError_t launch_of(const BatchForce& f, int grid, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(f.counter, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return e;
-    k_force_batch<LAW, ACC, POT><<<grid, kFBlock, 0, s>>>(f);
+    k_force_batch<LAW, ACC, POT, B, I><<<grid, B, 0, s>>>(f);
     return cudaGetLastError();
 }
 
-cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, cudaStream_t s) {
+template <int LAW>
+static int occ_law(bool acc, bool pot, int block, int ipt) {
+    if (!acc || pot) {
+        if (block != 128 || ipt != 2) return -1;
+        return acc ? occ_of<LAW, true, true, 128, 2>() : occ_of<LAW, false, true, 128, 2>();
+    }
+    if (block == 128) return ipt == 1 ? occ_of<LAW, true, false, 128, 1>() : occ_of<LAW, true, false, 128, 2>();
+    return ipt == 1 ? occ_of<LAW, true, false, 256, 1>() : occ_of<LAW, true, false, 256, 2>();
+}
+
+template <int LAW>
+static cudaError_t launch_law(const BatchForce& f, int grid, int block, int ipt, cudaStream_t s) {
+    const bool acc = f.ax != nullptr, pot = f.pot != nullptr;
+    if (!acc || pot) {
+        if (block != 128 || ipt != 2) return cudaErrorInvalidValue;
+        return acc ? launch_of<LAW, true, true, 128, 2>(f, grid, s)
+                   : launch_of<LAW, false, true, 128, 2>(f, grid, s);
+    }
+    if (block == 128)
+        return ipt == 1 ? launch_of<LAW, true, false, 128, 1>(f, grid, s)
+                        : launch_of<LAW, true, false, 128, 2>(f, grid, s);
+    return ipt == 1 ? launch_of<LAW, true, false, 256, 1>(f, grid, s)
+                    : launch_of<LAW, true, false, 256, 2>(f, grid, s);
+}
+
+int batch_ctas_per_sm(int law, bool acc, bool pot, int block, int ipt) {
+    if (!batch_shape_ok(block, ipt)) return -1;
+    return law == NB_LAW_PLUMMER ? occ_law<NB_LAW_PLUMMER>(acc, pot, block, ipt)
+                                 : occ_law<NB_LAW_SPLINE_G2>(acc, pot, block, ipt);
+}
+
+cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, int block, int ipt,
+                               cudaStream_t s) {
     const bool acc = f.ax != nullptr, pot = f.pot != nullptr;
     if (f.nitems <= 0 || grid <= 0 || (!acc && !pot)) return cudaSuccess;
-    if (law == NB_LAW_PLUMMER) {
-        if (!acc) return launch_fb<NB_LAW_PLUMMER, false, true>(f, grid, s);
-        return pot ? launch_fb<NB_LAW_PLUMMER, true, true>(f, grid, s)
-                   : launch_fb<NB_LAW_PLUMMER, true, false>(f, grid, s);
-    }
-    if (!acc) return launch_fb<NB_LAW_SPLINE_G2, false, true>(f, grid, s);
-    return pot ? launch_fb<NB_LAW_SPLINE_G2, true, true>(f, grid, s)
-               : launch_fb<NB_LAW_SPLINE_G2, true, false>(f, grid, s);
+    if (!batch_shape_ok(block, ipt)) return cudaErrorInvalidValue;
+    return law == NB_LAW_PLUMMER ? launch_law<NB_LAW_PLUMMER>(f, grid, block, ipt, s)
+                                 : launch_law<NB_LAW_SPLINE_G2>(f, grid, block, ipt, s);
 }
 
 // ---------------------------------------------------------------------------
@@ -621,9 +640,9 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
                               const double* bbox, const int32_t* perm, const double* x,
                               const double* y, const double* z, const double* m, float4* pack,
-                              dvec4* origin, cudaStream_t s) {
+                              dvec4* origin, float4* ext, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
-    k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, bbox, perm, x, y, z, m, pack, origin);
+    k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, bbox, perm, x, y, z, m, pack, origin, ext);
     return cudaGetLastError();
 }
 

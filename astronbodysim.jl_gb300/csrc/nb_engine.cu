@@ -58,6 +58,7 @@ struct nb_engine {
     cudaStream_t stream = nullptr;
     int nsm = 0;
     int occ_acc = 1, occ_pot = 1;
+    int fblock = 128, fipt = 2;  // batch force launch shape
     std::string err;
 
     // device arena
@@ -71,6 +72,7 @@ struct nb_engine {
     void* sort_scratch = nullptr;
     float4* pack = nullptr;
     nb::dvec4* origin = nullptr;
+    float4* ext = nullptr;
     int32_t* tile_rank = nullptr;
     nb::SysDesc* sysdesc = nullptr;
     nb::BatchSys* batchsys = nullptr;
@@ -84,6 +86,7 @@ struct nb_engine {
     int32_t* counter = nullptr;
     uint32_t* derr = nullptr;
     int64_t tile_cap = 0;
+    int64_t item_cap = 0;
 
     // host bookkeeping
     std::map<int64_t, int64_t> free_ranges;  // offset -> size
@@ -201,7 +204,8 @@ int rebuild(nb_engine* e) {
         d.n = (int32_t)q.n;
         d.tile_off = (int32_t)toff;
         d.ntiles = (int32_t)nt;
-        d.nblocks = (int32_t)((q.n + nb::batch_block_targets() - 1) / nb::batch_block_targets());
+        const int32_t bt = nb::batch_block_targets(e->fblock, e->fipt);
+        d.nblocks = (int32_t)((q.n + bt - 1) / bt);
         for (int k = 0; k < 6; ++k) d.soft[k] = q.soft;
         sd[r] = d;
         bs[r] = nb::BatchSys{q.aoff, soff, (int32_t)q.n, slots[r]};
@@ -223,6 +227,7 @@ int rebuild(nb_engine* e) {
     for (int32_t r : order)
         for (int32_t b = 0; b < sd[r].nblocks; ++b) items.push_back(make_int2(r, b));
     if (toff > e->tile_cap) return efail(e, NB_ERR_STATE, "tile capacity exceeded");
+    if ((int64_t)items.size() > e->item_cap) return efail(e, NB_ERR_STATE, "work-item capacity exceeded");
     if (R > 0) {
         NE_CK(cudaMemcpy(e->sysdesc, sd.data(), sizeof(nb::SysDesc) * R, cudaMemcpyHostToDevice));
         NE_CK(cudaMemcpy(e->batchsys, bs.data(), sizeof(nb::BatchSys) * R, cudaMemcpyHostToDevice));
@@ -259,6 +264,7 @@ nb::BatchForce force_args(nb_engine* e, const int2* items, int32_t nitems) {
     f.perm = e->lperm;
     f.pack = e->pack;
     f.origin = e->origin;
+    f.ext = e->ext;
     f.x = e->x;
     f.y = e->y;
     f.z = e->z;
@@ -297,7 +303,7 @@ cudaError_t enqueue_sort_pack(nb_engine* e, cudaStream_t s, bool force_all) {
                                     e->lperm, s);
     if (r != cudaSuccess) return r;
     return nb::launch_batch_pack(e->tile_rank, e->ntiles_total, e->sysdesc, e->bbox, e->lperm, e->x,
-                                 e->y, e->z, e->m, e->pack, e->origin, s);
+                                 e->y, e->z, e->m, e->pack, e->origin, e->ext, s);
 }
 
 // One KDK step of every running system (enqueue only).
@@ -307,7 +313,8 @@ cudaError_t enqueue_step(nb_engine* e, cudaStream_t s) {
     if (r != cudaSuccess) return r;
     r = enqueue_sort_pack(e, s, false);
     if (r != cudaSuccess) return r;
-    r = nb::launch_force_batch(e->p.law, force_args(e, e->items, e->nitems), e->occ_acc * e->nsm, s);
+    r = nb::launch_force_batch(e->p.law, force_args(e, e->items, e->nitems), e->occ_acc * e->nsm,
+                               e->fblock, e->fipt, s);
     if (r != cudaSuccess) return r;
     r = nb::launch_batch_kick(e->vx, e->vy, e->vz, e->ax, e->ay, e->az, e->sysid, e->dt_slot,
                               e->fac_step, e->high_water, s);
@@ -394,7 +401,7 @@ int start_systems(nb_engine* e, const std::vector<int32_t>& slots) {
     // keep their order (their schedule must not depend on admissions).
     NE_CK(enqueue_sort_pack(e, e->stream, false));
     NE_CK(nb::launch_force_batch(e->p.law, force_args(e, e->items_new, (int32_t)items.size()),
-                                 e->occ_acc * e->nsm, e->stream));
+                                 e->occ_acc * e->nsm, e->fblock, e->fipt, e->stream));
     return half_kick(e, slots, 0.5);
 }
 
@@ -437,7 +444,8 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     if (!p || !out) return NB_ERR_INVALID_ARG;
     *out = nullptr;
     if (p->max_particles <= 0 || p->max_particles > 0x7fffffffLL || p->max_systems <= 0 ||
-        (p->law != NB_LAW_SPLINE_G2 && p->law != NB_LAW_PLUMMER))
+        (p->law != NB_LAW_SPLINE_G2 && p->law != NB_LAW_PLUMMER) ||
+        !nb::batch_shape_ok(p->block > 0 ? p->block : 128, p->i_per_thread > 0 ? p->i_per_thread : 2))
         return NB_ERR_INVALID_ARG;
     nb_engine* e = new (std::nothrow) nb_engine();
     if (!e) return NB_ERR_OOM;
@@ -450,7 +458,9 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
         return NB_ERR_CUDA;
     }
     cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->dev);
-    e->occ_acc = nb::batch_ctas_per_sm(p->law, true, false);
+    e->fblock = p->block > 0 ? p->block : 128;
+    e->fipt = p->i_per_thread > 0 ? p->i_per_thread : 2;
+    e->occ_acc = nb::batch_ctas_per_sm(p->law, true, false, e->fblock, e->fipt);
     nb::prepare_batch_sort_small();
     const int64_t P = p->max_particles, S = p->max_systems;
     e->tile_cap = P / kTile + S;
@@ -468,12 +478,15 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     size_t o_sort = take(nb::sort_scratch_bytes(P));
     size_t o_pack = take(sizeof(float4) * kTile * (size_t)e->tile_cap);
     size_t o_orig = take(sizeof(nb::dvec4) * (size_t)e->tile_cap);
+    size_t o_ext = take(sizeof(float4) * (size_t)e->tile_cap);
     size_t o_trank = take(sizeof(int32_t) * (size_t)e->tile_cap);
     size_t o_sd = take(sizeof(nb::SysDesc) * S), o_bs = take(sizeof(nb::BatchSys) * S);
     size_t o_ros = take(sizeof(int32_t) * S), o_bbox = take(sizeof(double) * 6 * S);
     size_t o_dt = take(sizeof(double) * S), o_fs = take(sizeof(double) * S);
     size_t o_fo = take(sizeof(double) * S);
-    size_t o_it = take(sizeof(int2) * (size_t)e->tile_cap), o_itn = take(sizeof(int2) * (size_t)e->tile_cap);
+    // work items: at most one per i-block of the smallest block (128 targets) per system
+    e->item_cap = P / 128 + S;
+    size_t o_it = take(sizeof(int2) * (size_t)e->item_cap), o_itn = take(sizeof(int2) * (size_t)e->item_cap);
     size_t o_cnt = take(sizeof(int32_t) * 4), o_err = take(sizeof(uint32_t) * 4);
     if (cudaMalloc(&e->arena, off) != cudaSuccess) {
         cudaStreamDestroy(e->stream);
@@ -490,6 +503,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     e->sort_scratch = b + o_sort;
     e->pack = (float4*)(b + o_pack);
     e->origin = (nb::dvec4*)(b + o_orig);
+    e->ext = (float4*)(b + o_ext);
     e->tile_rank = (int32_t*)(b + o_trank);
     e->sysdesc = (nb::SysDesc*)(b + o_sd);
     e->batchsys = (nb::BatchSys*)(b + o_bs);

@@ -37,7 +37,8 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
                                                  const double* __restrict__ m, int64_t n,
                                                  const int32_t* __restrict__ perm,
                                                  float4* __restrict__ pack,
-                                                 dvec4* __restrict__ origin) {
+                                                 dvec4* __restrict__ origin,
+                                                 float4* __restrict__ ext) {
     __shared__ double red[6][kTileJ / 32];
     const int64_t i = (int64_t)blockIdx.x * kTileJ + threadIdx.x;
     const bool valid = i < n;
@@ -102,16 +103,25 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
     if (threadIdx.x == 0) {
         const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
         origin[blockIdx.x] = make_dvec4(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
+        // Half extents of the box for the near test, rounded up and enlarged to
+        // cover the rounding of the FP32 relative coordinates (the test must
+        // never under-estimate them).
+        const double amax = fmax(0.5 * ex, fmax(0.5 * ey, 0.5 * ez));
+        const double slack = 4.0e-7 * amax;
+        ext[blockIdx.x] = make_float4(__double2float_ru(0.5 * ex * (1.0 + 1e-5) + slack),
+                                      __double2float_ru(0.5 * ey * (1.0 + 1e-5) + slack),
+                                      __double2float_ru(0.5 * ez * (1.0 + 1e-5) + slack),
+                                      __double2float_ru(0.5 * sqrt(ex * ex + ey * ey + ez * ez)));
     }
 }
 
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
                         int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
-                        cudaStream_t s) {
+                        float4* ext, cudaStream_t s) {
     if (tile_j != kTileJ) return cudaErrorInvalidValue;
     if (n <= 0) return cudaSuccess;
     const int64_t ntiles = (n + kTileJ - 1) / kTileJ;
-    k_pack<<<(unsigned)ntiles, kTileJ, 0, s>>>(x, y, z, m, n, perm, pack, origin);
+    k_pack<<<(unsigned)ntiles, kTileJ, 0, s>>>(x, y, z, m, n, perm, pack, origin, ext);
     return cudaGetLastError();
 }
 
@@ -229,16 +239,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
         // lies farther than (tile radius + h) from the tile origin, no pair of
         // this tile can have r < h and the branch-free loop runs.
         bool near = false;
-        if (LAW == NB_LAW_SPLINE_G2) {
-            const float R = (float)o.w;
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const float d2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
-                const float lim = (R + hh[k]) * 1.0001f;
-                near |= (pidx[k] >= 0) && (d2 <= lim * lim);
-            }
-            near = __any_sync(0xffffffffu, near);
-        }
+        if (LAW == NB_LAW_SPLINE_G2) near = warp_near<IPT>(src.ext[t_lo + t], xr, yr, zr, hh, pidx);
         if (near)
             pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
         else

@@ -214,16 +214,8 @@ __global__ void __launch_bounds__(kWBlock, (ACC && !POT) ? 8 : 1) k_force_workli
         }
         const float4* b = &buf[st * kTileJ];
         bool near = false;
-        if (LAW == NB_LAW_SPLINE_G2) {
-            const float R = (float)o.w;
-#pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const float d2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
-                const float lim = (R + hh[k]) * 1.0001f;
-                near |= (pidx[k] >= 0) && (d2 <= lim * lim);
-            }
-            near = __any_sync(0xffffffffu, near);
-        }
+        if (LAW == NB_LAW_SPLINE_G2)
+            near = warp_near<IPT>(w.ext[cur.tile_off + cur.t], xr, yr, zr, hh, pidx);
         if (near)
             pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
         else

@@ -81,6 +81,7 @@ struct Targets {
 struct Sources32 {
     const float4* pack;
     const dvec4* origin;
+    const float4* ext;  // per tile: half extents of the box (x, y, z) and half diagonal
     int32_t ntiles;
     int32_t tile_j;
     // j-split: each i-block's tiles are shared by jsplit CTAs, which write
@@ -123,6 +124,7 @@ struct WorkList {
     const int32_t* perm;       // otherwise target slot q of system s is particle perm[off + q]
     const float4* pack;
     const dvec4* origin;
+    const float4* ext;
     const double* x;
     const double* y;
     const double* z;
@@ -163,6 +165,7 @@ struct BatchForce {
     const int32_t* perm;  // sorted slot -> arena particle
     const float4* pack;
     const dvec4* origin;
+    const float4* ext;
     const double* x;
     const double* y;
     const double* z;
@@ -175,10 +178,12 @@ struct BatchForce {
     uint32_t* err;
 };
 
-cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, cudaStream_t s);
+cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, int block, int ipt,
+                               cudaStream_t s);
 cudaError_t launch_fill_i32(int32_t* a, int64_t n, int32_t v, cudaStream_t s);
-int batch_ctas_per_sm(int law, bool acc, bool pot);
-int batch_block_targets();
+int batch_ctas_per_sm(int law, bool acc, bool pot, int block, int ipt);
+bool batch_shape_ok(int block, int ipt);
+int batch_block_targets(int block, int ipt);
 cudaError_t launch_batch_bbox(const BatchSys* bs, int32_t nrank, const double* x, const double* y,
                               const double* z, double* bbox, cudaStream_t s);
 cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot, const double* bbox,
@@ -187,7 +192,7 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
                               const double* bbox, const int32_t* perm, const double* x,
                               const double* y, const double* z, const double* m, float4* pack,
-                              dvec4* origin, cudaStream_t s);
+                              dvec4* origin, float4* ext, cudaStream_t s);
 int batch_small_sort_limit();
 cudaError_t prepare_batch_sort_small();
 cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t max_small_n,
@@ -208,7 +213,7 @@ cudaError_t launch_batch_kick(double* vx, double* vy, double* vz, const double* 
 // Launch helpers implemented in the .cu files.
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
                         int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
-                        cudaStream_t s);
+                        float4* ext, cudaStream_t s);
 // Morton-order permutation of the particles (nb_sort.cu); scratch of
 // sort_scratch_bytes(n) bytes.
 size_t sort_scratch_bytes(int64_t n);

@@ -38,7 +38,8 @@ constexpr size_t al256(size_t v) { return (v + 255) / 256 * 256; }
 constexpr size_t kOffPerm = 0;
 constexpr size_t kOffPack = kOffPerm + al256(sizeof(int32_t) * kNoAllocMaxParticles);
 constexpr size_t kOffOrigin = kOffPack + al256(sizeof(float4) * kNoAllocMaxParticles);
-constexpr size_t kOffErr = kOffOrigin + al256(sizeof(nb::dvec4) * (kNoAllocMaxParticles / kTile));
+constexpr size_t kOffExt = kOffOrigin + al256(sizeof(nb::dvec4) * (kNoAllocMaxParticles / kTile));
+constexpr size_t kOffErr = kOffExt + al256(sizeof(float4) * (kNoAllocMaxParticles / kTile));
 constexpr size_t kOffSort = kOffErr + 256;
 // Upper bound of the radix-sort scratch for kNoAllocMaxParticles (two key
 // buffers, one value buffer, 256 digit counts per 2048-particle block, bounding
@@ -119,6 +120,7 @@ extern "C" int nb_force_noalloc(int64_t n, const double* x, const double* y, con
     int32_t* perm = reinterpret_cast<int32_t*>(b + kOffPerm);
     float4* pack = reinterpret_cast<float4*>(b + kOffPack);
     nb::dvec4* origin = reinterpret_cast<nb::dvec4*>(b + kOffOrigin);
+    float4* ext = reinterpret_cast<float4*>(b + kOffExt);
     uint32_t* err = reinterpret_cast<uint32_t*>(b + kOffErr);
     void* sort_scratch = b + kOffSort;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -126,9 +128,9 @@ extern "C" int nb_force_noalloc(int64_t n, const double* x, const double* y, con
     // The error word is the only state that must start at zero.
     e = cudaMemsetAsync(err, 0, sizeof(uint32_t), s);
     if (e == cudaSuccess) e = nb::launch_morton_sort(x, y, z, n, sort_scratch, perm, s);
-    if (e == cudaSuccess) e = nb::launch_pack(x, y, z, m, n, perm, kTile, pack, origin, s);
+    if (e == cudaSuccess) e = nb::launch_pack(x, y, z, m, n, perm, kTile, pack, origin, ext, s);
     if (e == cudaSuccess) {
-        nb::Sources32 src{pack, origin, (int32_t)((n + kTile - 1) / kTile), kTile};
+        nb::Sources32 src{pack, origin, ext, (int32_t)((n + kTile - 1) / kTile), kTile};
         nb::Targets tg{};
         tg.x = x;
         tg.y = y;

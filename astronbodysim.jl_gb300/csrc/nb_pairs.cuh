@@ -47,6 +47,26 @@ __device__ __forceinline__ void spline_close(float r2, float rinv, float m, floa
 // pair_loop_checked: scalar, tests r < h per pair (spline slow path, j == i).
 // Both accumulate per-tile partials; pot accumulates +m/r (negated later).
 // ---------------------------------------------------------------------------
+// Warp-uniform choice of the pair loop: a pair of this tile can have r < h
+// only for a target whose distance to the tile's box (half extents e.x, e.y,
+// e.z about the tile origin, enlarged for rounding) is at most h.  When no
+// target of the warp is that close, the branch-free loop runs.
+template <int IPT>
+__device__ __forceinline__ bool warp_near(const float4 e, const float* xr, const float* yr,
+                                          const float* zr, const float* hh, const int32_t* pidx) {
+    bool near = false;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const float bx = fmaxf(fabsf(xr[k]) - e.x, 0.0f);
+        const float by = fmaxf(fabsf(yr[k]) - e.y, 0.0f);
+        const float bz = fmaxf(fabsf(zr[k]) - e.z, 0.0f);
+        const float d2 = fmaf(bx, bx, fmaf(by, by, bz * bz));
+        const float lim = hh[k] * 1.0001f;
+        near |= (pidx[k] >= 0) && (d2 <= lim * lim);
+    }
+    return __any_sync(0xffffffffu, near);
+}
+
 template <int LAW, bool ACC, bool POT, int IPT>
 __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, const float* xr,
                                                const float* yr, const float* zr, const float* h2,
@@ -100,19 +120,24 @@ __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, 
                                                   const float* yr, const float* zr,
                                                   const float* hh, const float* h2, float* ax,
                                                   float* ay, float* az, float* ap) {
-    // Same packed FP32x2 arithmetic as pair_loop_fast; each source pair is then
-    // tested for r < h on both halves and, when any lane of the warp has such a
-    // pair, the spline replaces the Newtonian factor of those halves.
+    // Two passes over the tile.  Pass 1 is the packed FP32x2 loop of
+    // pair_loop_fast with the Newtonian factor of every r < h half set to zero
+    // by a select (so the self pair, r = 0, adds nothing), and a per-thread
+    // flag of whether such a half occurred.  Pass 2 runs only when a lane of
+    // the warp saw one: it walks the tile again and adds the spline terms of
+    // the r < h pairs.
     float2 nx[IPT], ny[IPT], nz[IPT];
     float2 sx[IPT], sy[IPT], sz[IPT], sp[IPT];
+    bool seen[IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         nx[k] = make_float2(-xr[k], -xr[k]);
         ny[k] = make_float2(-yr[k], -yr[k]);
         nz[k] = make_float2(-zr[k], -zr[k]);
         sx[k] = sy[k] = sz[k] = sp[k] = make_float2(0.0f, 0.0f);
+        seen[k] = false;
     }
-#pragma unroll 1
+#pragma unroll 4
     for (int p = 0; p < kTileJ / 2; ++p) {
         const float4 A = b[2 * p];
         const float4 B = b[2 * p + 1];
@@ -127,17 +152,58 @@ __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, 
             const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
             float2 mp = __fmul2_rn(qm, rinv);
             float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
-            const bool close = (r2.x < h2[k]) | (r2.y < h2[k]);
-            if (__any_sync(0xffffffffu, close)) {
-                if (r2.x < h2[k]) spline_close(r2.x, rinv.x, qm.x, hh[k], mr3.x, mp.x);
-                if (r2.y < h2[k]) spline_close(r2.y, rinv.y, qm.y, hh[k], mr3.y, mp.y);
-            }
+            const bool cx = r2.x < h2[k], cy = r2.y < h2[k];
+            seen[k] |= cx | cy;
+            mr3.x = cx ? 0.0f : mr3.x;
+            mr3.y = cy ? 0.0f : mr3.y;
             if (ACC) {
                 sx[k] = __ffma2_rn(dx, mr3, sx[k]);
                 sy[k] = __ffma2_rn(dy, mr3, sy[k]);
                 sz[k] = __ffma2_rn(dz, mr3, sz[k]);
             }
-            if (POT) sp[k] = __fadd2_rn(sp[k], mp);
+            if (POT) {
+                mp.x = cx ? 0.0f : mp.x;
+                mp.y = cy ? 0.0f : mp.y;
+                sp[k] = __fadd2_rn(sp[k], mp);
+            }
+        }
+    }
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) any |= seen[k];
+    if (__any_sync(0xffffffffu, any)) {
+#pragma unroll 1
+        for (int p = 0; p < kTileJ / 2; ++p) {
+            const float4 A = b[2 * p];
+            const float4 B = b[2 * p + 1];
+            const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+            const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float2 dx = __fadd2_rn(qx, nx[k]);
+                const float2 dy = __fadd2_rn(qy, ny[k]);
+                const float2 dz = __fadd2_rn(qz, nz[k]);
+                const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                const bool cx = r2.x < h2[k], cy = r2.y < h2[k];
+                if (__any_sync(0xffffffffu, cx | cy)) {
+                    if (cx) {
+                        float mr3, mp;
+                        spline_close(r2.x, rsqrt_approx(r2.x), qm.x, hh[k], mr3, mp);
+                        sx[k].x = fmaf(dx.x, mr3, sx[k].x);
+                        sy[k].x = fmaf(dy.x, mr3, sy[k].x);
+                        sz[k].x = fmaf(dz.x, mr3, sz[k].x);
+                        sp[k].x += mp;
+                    }
+                    if (cy) {
+                        float mr3, mp;
+                        spline_close(r2.y, rsqrt_approx(r2.y), qm.y, hh[k], mr3, mp);
+                        sx[k].y = fmaf(dx.y, mr3, sx[k].y);
+                        sy[k].y = fmaf(dy.y, mr3, sy[k].y);
+                        sz[k].y = fmaf(dz.y, mr3, sz[k].y);
+                        sp[k].y += mp;
+                    }
+                }
+            }
         }
     }
 #pragma unroll

@@ -387,7 +387,7 @@ def run_ensemble(nb, args, rank=0, local=0):
     ens = nb.ensemble_systems(args.batch_systems, seed=11 + rank)
     tot = sum(d["pos"].shape[0] for d, _ in ens)
     eng = nb.Engine(max_particles=tot + 4096, max_systems=args.batch_systems,
-                    max_steps_per_call=args.batch_steps, device=local, law=args.law)
+                    max_steps_per_call=args.batch_steps, device=local, law=args.law, tuning="auto")
     for d, eps in ens:
         eng.submit(d, eps, 1e-3, args.batch_steps)
     del ens
@@ -400,6 +400,7 @@ def run_ensemble(nb, args, rank=0, local=0):
             "systems": args.batch_systems, "particles": tot, "steps": args.batch_steps,
             "interactions": st["interactions"], "gpu_s": st["gpu_ms"] / 1e3,
             "wall_s_incl_admission_and_retirement": t_batch_wall,
+            "force_shape": "%dx%d (block x targets/thread)" % eng.shape,
             "workload": "N log-uniform [64, 8192], half Plummer / half Hernquist (a=1, r<100a), "
                         "m=1/N, eps U[1e-3, 1e-2], mixed, %d KDK steps dt=1e-3, one CUDA graph "
                         "per step" % args.batch_steps}
@@ -538,6 +539,7 @@ def main():
 
         for law in ("spline", "plummer"):
             autotune.save(autotune.tune([1 << k for k in range(12, 21)], law=law, reps=3))
+        autotune.save_batch(autotune.tune_batch(law="spline"))
         print(json.dumps(autotune.load()), flush=True)
         return 0
     return run_gpu(args)

@@ -257,6 +257,9 @@ typedef struct nb_engine_params {
     int64_t max_particles;      /* arena capacity: the footprint budget of admission */
     int32_t max_systems;        /* resident system slots */
     int32_t max_steps_per_call; /* steps between admission rounds in nb_engine_run (0 = 64) */
+    int32_t block;              /* tuning override: threads per CTA of the batch force (128, 256;
+                                   0 = 128) */
+    int32_t i_per_thread;       /* tuning override: targets per thread (1, 2; 0 = 2) */
 } nb_engine_params;
 
 #define NB_REQ_QUEUED 0

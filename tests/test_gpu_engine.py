@@ -159,3 +159,31 @@ def test_suspend_errors(nb):
         eng.fetch(rid, 500)  # not finished
     eng.cancel(rid)
     assert eng.poll(rid)[0] == nb._lib.NB_REQ_CANCELLED
+
+
+@pytest.mark.parametrize("shape", [(128, 1), (256, 1), (256, 2)])
+def test_engine_launch_shapes_agree(nb, shape):
+    """Every batch-force shape gives the default shape's trajectories to FP32
+    round-off, and stays mix-independent (bit-identical alone and in a mix)."""
+    ds = systems(nb, [300, 2000, 5000], seed=81)
+    dt, nsteps = 1e-3, 10
+    runs = {}
+    for sh in [(128, 2), shape]:
+        eng = nb.Engine(max_particles=1 << 15, max_systems=8, block=sh[0], i_per_thread=sh[1])
+        ids = [eng.submit(d, 0.01, dt, nsteps) for d in ds]
+        eng.run_until_idle()
+        runs[sh] = [eng.fetch(i, d["pos"].shape[0]) for i, d in zip(ids, ds)]
+    for a, b in zip(runs[(128, 2)], runs[shape]):
+        np.testing.assert_allclose(a["pos"], b["pos"], rtol=0, atol=1e-9)
+        np.testing.assert_allclose(a["vel"], b["vel"], rtol=0, atol=1e-7)
+    eng = nb.Engine(max_particles=1 << 15, max_systems=8, block=shape[0], i_per_thread=shape[1])
+    rid = eng.submit(ds[1], 0.01, dt, nsteps)
+    eng.run_until_idle()
+    alone = eng.fetch(rid, 2000)
+    np.testing.assert_array_equal(alone["pos"], runs[shape][1]["pos"])
+    np.testing.assert_array_equal(alone["vel"], runs[shape][1]["vel"])
+
+
+def test_engine_rejects_unknown_shape(nb):
+    with pytest.raises(nb.NbodyError):
+        nb.Engine(max_particles=1 << 12, max_systems=4, block=512, i_per_thread=1)
