@@ -246,6 +246,7 @@ __global__ void __launch_bounds__(kTileJ)
     // the sources are then re-expressed relative to it in FP64.  Everything
     // depends on this tile's particles only.
     __shared__ float red[6][kTileJ / 32];
+    __shared__ double mred[2][kTileJ / 32];
     __shared__ double cref[3];
     const int32_t g = blockIdx.x;
     const int32_t r = tile_rank[g];
@@ -281,10 +282,18 @@ __global__ void __launch_bounds__(kTileJ)
     for (int k = 0; k < 6; ++k)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    double mm[2] = {valid ? pm : 1e300, valid ? -pm : 1e300};  // smallest / largest mass
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mm[k] = fmin(mm[k], __shfl_xor_sync(0xffffffffu, mm[k], o));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0)
+    if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
+        mred[0][warp] = mm[0];
+        mred[1][warp] = mm[1];
+    }
     __syncthreads();
     float lo[3], hi[3];
 #pragma unroll
@@ -324,8 +333,15 @@ __global__ void __launch_bounds__(kTileJ)
         origin[g] = make_dvec4(ox, oy, oz, (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
         // box half extents for the near test, enlarged the same way
         const float slack = 4.0e-7f * amax;
+        // ext.w: the common source mass when all are equal, else 0
+        double mlo = mred[0][0], mhi = mred[1][0];
+        for (int w = 1; w < kTileJ / 32; ++w) {
+            mlo = fmin(mlo, mred[0][w]);
+            mhi = fmin(mhi, mred[1][w]);
+        }
+        const float mu = (mlo == -mhi && mlo > 0.0) ? (float)mlo : 0.0f;
         ext[g] = make_float4(0.5f * ex * (1.0f + 1e-5f) + slack, 0.5f * ey * (1.0f + 1e-5f) + slack,
-                             0.5f * ez * (1.0f + 1e-5f) + slack, rr);
+                             0.5f * ez * (1.0f + 1e-5f) + slack, mu);
     }
 }
 
@@ -439,7 +455,7 @@ __global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) 
             if (near)
                 pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
             else
-                pair_loop_fast<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap);
+                pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, f.ext[d.tile_off + t].w);
             __syncwarp();
             if (lane == 0) {
                 __threadfence_block();

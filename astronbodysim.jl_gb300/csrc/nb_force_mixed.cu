@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
                                                  float4* __restrict__ pack,
                                                  dvec4* __restrict__ origin,
                                                  float4* __restrict__ ext) {
-    __shared__ double red[6][kTileJ / 32];
+    __shared__ double red[8][kTileJ / 32];
     const int64_t i = (int64_t)blockIdx.x * kTileJ + threadIdx.x;
     const bool valid = i < n;
     double px = 0.0, py = 0.0, pz = 0.0, pm = 0.0;
@@ -50,36 +50,43 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
         pz = z[p];
         pm = m[p];
     }
-    double v[6];
+    // bounding box (v[0..5]) and the smallest / largest mass (v[6], -v[7])
+    double v[8];
     v[0] = valid ? px : 1e300;
     v[1] = valid ? py : 1e300;
     v[2] = valid ? pz : 1e300;
     v[3] = valid ? -px : 1e300;
     v[4] = valid ? -py : 1e300;
     v[5] = valid ? -pz : 1e300;
+    v[6] = valid ? pm : 1e300;
+    v[7] = valid ? -pm : 1e300;
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < 8; ++k) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
+        for (int k = 0; k < 8; ++k) red[k][warp] = v[k];
     }
     __syncthreads();
-    double lo[3], hi[3];
+    double lo[4], hi[4];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        double a = red[k][0], b = red[k + 3][0];
+    for (int k = 0; k < 4; ++k) {
+        const int ka = k < 3 ? k : 6, kb = k < 3 ? k + 3 : 7;
+        double a = red[ka][0], b = red[kb][0];
 #pragma unroll
         for (int w = 1; w < kTileJ / 32; ++w) {
-            a = fmin(a, red[k][w]);
-            b = fmin(b, red[k + 3][w]);
+            a = fmin(a, red[ka][w]);
+            b = fmin(b, red[kb][w]);
         }
         lo[k] = a;
         hi[k] = -b;
     }
+    // ext.w: the common mass of the tile's sources when all are equal (the
+    // far-tile loop then applies it once per tile), else 0.
+    const float mu = (lo[3] == hi[3] && lo[3] > 0.0) ? (float)lo[3] : 0.0f;
     // Every tile holds at least one particle (tiles cover [0, n)).
     const double ox = 0.5 * (lo[0] + hi[0]);
     const double oy = 0.5 * (lo[1] + hi[1]);
@@ -111,7 +118,7 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
         ext[blockIdx.x] = make_float4(__double2float_ru(0.5 * ex * (1.0 + 1e-5) + slack),
                                       __double2float_ru(0.5 * ey * (1.0 + 1e-5) + slack),
                                       __double2float_ru(0.5 * ez * (1.0 + 1e-5) + slack),
-                                      __double2float_ru(0.5 * sqrt(ex * ex + ey * ey + ez * ez)));
+                                      mu);
     }
 }
 
@@ -243,7 +250,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
         if (near)
             pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
         else
-            pair_loop_fast<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap);
+            pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, src.ext[t_lo + t].w);
 
         // Release stage s; the last warp out refills it with tile t + kStages.
         __syncwarp();

@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kWBlock, (ACC && !POT) ? 8 : 1) k_force_workli
         if (near)
             pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
         else
-            pair_loop_fast<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap);
+            pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, w.ext[cur.tile_off + cur.t].w);
 
         // Release stage st; the last warp out refills it with unit v + kStages.
         __syncwarp();

@@ -313,15 +313,16 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     return t;
 }
 
-// Bounded wait: gives up after ~timeout_ns of wall time (globaltimer) or an
-// iteration cap, whichever comes first.  Returns false on timeout.
+// Bounded wait: gives up after ~timeout_ns of wall time (globaltimer, read
+// after every try_wait, each of which suspends for at most a system-defined
+// slice) or an iteration cap, whichever comes first.  Returns false on timeout.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
                                                   uint64_t timeout_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (uint32_t it = 0; it < (1u << 26); ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 255u && globaltimer_ns() - t0 > timeout_ns) return false;
+        if (globaltimer_ns() - t0 > timeout_ns) return false;
     }
     return false;
 }

@@ -67,52 +67,90 @@ __device__ __forceinline__ bool warp_near(const float4 e, const float* xr, const
     return __any_sync(0xffffffffu, near);
 }
 
-template <int LAW, bool ACC, bool POT, int IPT>
+// Branch-free loop for far tiles.  UNI: every source of the tile has the same
+// mass mu (flagged by the pack in ext.w), which is then applied once to the
+// tile's partial sums instead of once per pair (one FP32 operation less per
+// interaction).
+template <int LAW, bool ACC, bool POT, int IPT, bool UNI = false>
 __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, const float* xr,
                                                const float* yr, const float* zr, const float* h2,
-                                               float* ax, float* ay, float* az, float* ap) {
+                                               float* ax, float* ay, float* az, float* ap,
+                                               float mu = 1.0f) {
+    // With one target per thread the sums are split over two sets (even and
+    // odd source pairs) so that consecutive accumulating FMAs do not wait on
+    // each other; with more targets per thread they are independent already.
+    constexpr int NA = (IPT == 1) ? 2 : 1;
     float2 nx[IPT], ny[IPT], nz[IPT], e2[IPT];
-    float2 sx[IPT], sy[IPT], sz[IPT], sp[IPT];
+    float2 sx[NA][IPT], sy[NA][IPT], sz[NA][IPT], sp[NA][IPT];
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         nx[k] = make_float2(-xr[k], -xr[k]);
         ny[k] = make_float2(-yr[k], -yr[k]);
         nz[k] = make_float2(-zr[k], -zr[k]);
         e2[k] = make_float2(h2[k], h2[k]);
-        sx[k] = sy[k] = sz[k] = sp[k] = make_float2(0.0f, 0.0f);
-    }
-#pragma unroll 4
-    for (int p = 0; p < kTileJ / 2; ++p) {
-        const float4 A = b[2 * p];
-        const float4 B = b[2 * p + 1];
-        const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
-        const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            const float2 dx = __fadd2_rn(qx, nx[k]);
-            const float2 dy = __fadd2_rn(qy, ny[k]);
-            const float2 dz = __fadd2_rn(qz, nz[k]);
-            float2 r2 = (LAW == NB_LAW_PLUMMER) ? __ffma2_rn(dz, dz, e2[k]) : __fmul2_rn(dz, dz);
-            r2 = __ffma2_rn(dy, dy, r2);
-            r2 = __ffma2_rn(dx, dx, r2);
-            const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-            const float2 mp = __fmul2_rn(qm, rinv);
-            if (ACC) {
-                const float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
-                sx[k] = __ffma2_rn(dx, mr3, sx[k]);
-                sy[k] = __ffma2_rn(dy, mr3, sy[k]);
-                sz[k] = __ffma2_rn(dz, mr3, sz[k]);
+        for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll (4 / NA)
+    for (int p = 0; p < kTileJ / 2; p += NA) {
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+            const float4 A = b[2 * (p + u)];
+            const float4 B = b[2 * (p + u) + 1];
+            const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+            const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float2 dx = __fadd2_rn(qx, nx[k]);
+                const float2 dy = __fadd2_rn(qy, ny[k]);
+                const float2 dz = __fadd2_rn(qz, nz[k]);
+                float2 r2 = (LAW == NB_LAW_PLUMMER) ? __ffma2_rn(dz, dz, e2[k]) : __fmul2_rn(dz, dz);
+                r2 = __ffma2_rn(dy, dy, r2);
+                r2 = __ffma2_rn(dx, dx, r2);
+                const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+                const float2 mp = UNI ? rinv : __fmul2_rn(qm, rinv);
+                if (ACC) {
+                    const float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
+                    sx[u][k] = __ffma2_rn(dx, mr3, sx[u][k]);
+                    sy[u][k] = __ffma2_rn(dy, mr3, sy[u][k]);
+                    sz[u][k] = __ffma2_rn(dz, mr3, sz[u][k]);
+                }
+                if (POT) sp[u][k] = __fadd2_rn(sp[u][k], mp);
             }
-            if (POT) sp[k] = __fadd2_rn(sp[k], mp);
         }
     }
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-        ax[k] += sx[k].x + sx[k].y;
-        ay[k] += sy[k].x + sy[k].y;
-        az[k] += sz[k].x + sz[k].y;
-        ap[k] += sp[k].x + sp[k].y;
+        float tx = 0.0f, ty = 0.0f, tz = 0.0f, tp = 0.0f;
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+            tx += sx[u][k].x + sx[u][k].y;
+            ty += sy[u][k].x + sy[u][k].y;
+            tz += sz[u][k].x + sz[u][k].y;
+            tp += sp[u][k].x + sp[u][k].y;
+        }
+        if (UNI) {
+            tx *= mu;
+            ty *= mu;
+            tz *= mu;
+            tp *= mu;
+        }
+        ax[k] += tx;
+        ay[k] += ty;
+        az[k] += tz;
+        ap[k] += tp;
     }
+}
+
+// Far-tile dispatch: the uniform-mass loop when the pack flagged the tile.
+template <int LAW, bool ACC, bool POT, int IPT>
+__device__ __forceinline__ void pair_loop_far(const float4* __restrict__ b, const float* xr,
+                                              const float* yr, const float* zr, const float* h2,
+                                              float* ax, float* ay, float* az, float* ap, float mu) {
+    if (mu > 0.0f)
+        pair_loop_fast<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, h2, ax, ay, az, ap, mu);
+    else
+        pair_loop_fast<LAW, ACC, POT, IPT, false>(b, xr, yr, zr, h2, ax, ay, az, ap);
 }
 
 template <int LAW, bool ACC, bool POT, int IPT>

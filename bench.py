@@ -126,6 +126,21 @@ def cpu_oracle_rate(data, n_targets, seed=7, nthreads=0):
     return n_targets * data["pos"].shape[0] / dt, dt, oracle.max_threads() if nthreads == 0 else nthreads
 
 
+def replica_rates(ws, steps, e2e_steps, n, total_s, t_e2e, device):
+    """Whole-job rates of ws independent replicas (one system of n particles
+    per rank, no data-path collective): the job time is the slowest rank's
+    (MAX over ranks), and the job did ws x steps x n^2 interactions."""
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([total_s, t_e2e], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s, t_e2e = float(t[0]), float(t[1])
+    pairs = float(n) * float(n)
+    return (ws * steps * pairs / total_s / 1e9, ws * e2e_steps * pairs / t_e2e / 1e9, total_s, t_e2e)
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -240,6 +255,8 @@ def run_gpu(args):
             e1.record(stream)
         ev.append((e0, e1))
     torch.cuda.synchronize(dev)
+    if ws > 1:
+        torch.distributed.barrier()
     t_wall = time.perf_counter() - t_wall0
     step_ms = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(step_ms)
@@ -312,16 +329,11 @@ def run_gpu(args):
         serve_stats["arena_particles"] = args.serve_particles
 
     # ---- aggregate over ranks (replicas) -----------------------------------
-    total_s = total_ms / 1e3
-    if ws > 1:
-        t = torch.tensor([total_s, t_e2e], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_s, t_e2e = float(t[0]), float(t[1])
+    value, e2e_value, total_s, t_e2e = replica_rates(ws, args.steps, args.e2e_steps, n,
+                                                     total_ms / 1e3, t_e2e, dev)
     pairs = float(n) * float(n)
-    value = ws * args.steps * pairs / total_s / 1e9
     if batch is not None:
         batch["vs_single_system"] = batch["value"] / (value / ws)
-    e2e_value = ws * args.e2e_steps * pairs / t_e2e / 1e9
 
     if rank == 0:
         peaks = measured_peaks()
@@ -428,6 +440,60 @@ def energy_drift_pair(nb, law, device, n=32768, steps=10):
     return out
 
 
+def run_plummer4096(args):
+    """The oracle-sized case: Plummer N = 4096 (G = M = a = 1), eps = 0.01, both
+    laws; force + potential against the oracle, then 100 KDK steps at dt = 1e-3
+    (energy drift), on the GPU (mixed and plain FP64) and in the oracle."""
+    import torch
+
+    import astronbodysim as nb
+    from oracle import oracle
+
+    n, h, dt, nsteps = 4096, 0.01, 1e-3, 100
+    d = nb.plummer(n, seed=1)
+    out = {"mode": "plummer4096", "n": n, "eps": h, "dt": dt, "steps": nsteps, "unit": UNIT}
+    for law in ("spline", "plummer"):
+        olaw = oracle.LAW_SPLINE_G2 if law == "spline" else oracle.LAW_PLUMMER
+        a_ref, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], h, law=olaw)
+        o = oracle.OracleSim(d["pos"], d["vel"], d["mass"], soft=[h] * 6, dt=dt, time_end=1.0, law=olaw)
+        o.compute_potential()
+        od0 = o.diagnostics()
+        t0 = time.perf_counter()
+        o.run_begin()
+        o.step(nsteps)
+        o.run_end()
+        t_or = time.perf_counter() - t0
+        o.compute_potential()
+        od1 = o.diagnostics()
+        e0, e1 = od0["K"] + od0["W"], od1["K"] + od1["W"]
+        res = {"oracle": {"energy_rel_drift": (e1 - e0) / abs(e0), "wall_s_100_steps": t_or,
+                          "g_interactions_per_s": (nsteps + 1) * n * n / t_or / 1e9,
+                          "cores": oracle.max_threads()}}
+        for prec in ("mixed", "fp64"):
+            sim = nb.Simulation(d, ForceSofteningTable=[h] * 6, TimeStep=dt, TimeEnd=1.0,
+                                precision=prec, law=law)
+            nb.compute_force(sim, want_potential=True)
+            g = nb.get_all_data(sim)
+            ea = np.linalg.norm(g["acc"] - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+            ep = np.abs(g["pot"] - p_ref) / np.abs(p_ref)
+            dg0 = nb.diagnostics(sim)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            nb.run(sim, nsteps=nsteps)
+            torch.cuda.synchronize()
+            t_gpu = time.perf_counter() - t0
+            dg1 = nb.diagnostics(sim)
+            eg0, eg1 = dg0["K"] + dg0["W"], dg1["K"] + dg1["W"]
+            res[prec] = {"force_rel_median": float(np.median(ea)), "force_rel_p99": float(np.quantile(ea, 0.99)),
+                         "force_rel_max": float(ea.max()), "pot_rel_median": float(np.median(ep)),
+                         "energy_rel_drift": (eg1 - eg0) / abs(eg0), "wall_s_100_steps": t_gpu,
+                         "pos_max_abs_diff_vs_oracle": float(np.abs(nb.get_all_data(sim)["pos"] - o.pos).max())}
+            sim.close()
+        out[law] = res
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_collision(args):
     """Two Hernquist spheres on a parabolic approach, adaptive power-of-two bins
     with dt_i = eta sqrt(eps / |a_i|) (eta 0.025, dt_max 1e-2), eps 5e-3.
@@ -516,7 +582,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-particles", type=int, default=1 << 22)
-    ap.add_argument("--mode", default="bench", choices=["bench", "serve", "collision", "tune", "ensemble"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "serve", "collision", "tune", "ensemble",
+                                                         "plummer4096"])
     ap.add_argument("--n-each", type=int, default=1 << 20)
     ap.add_argument("--base-steps", type=int, default=2)
     ap.add_argument("--fp64-compare", action="store_true")
@@ -527,6 +594,8 @@ def main():
         return run_serve(args)
     if args.mode == "collision":
         return run_collision(args)
+    if args.mode == "plummer4096":
+        return run_plummer4096(args)
     if args.mode == "ensemble":
         import astronbodysim as nb
 

@@ -309,6 +309,14 @@ int nb_engine_get_stats(nb_engine *e, nb_engine_stats *out);
 int nb_engine_drain_done(nb_engine *e, int64_t *ids, int64_t cap, int64_t *count);
 const char *nb_engine_last_error(nb_engine *e);
 
+/* Self-test of the bounded-wait path (no counterpart in the reference): one
+ * warp on `device` waits on an mbarrier that nothing completes, gives up after
+ * timeout_ns (at most 2 s) exactly as the force kernels do on a copy that
+ * never lands, records the timeout in a device error word and returns.
+ * Returns NB_ERR_TIMEOUT (the expected outcome) with the time waited in
+ * *waited_ms; the device context stays usable. */
+int nb_selftest_wait_timeout(int device, int64_t timeout_ns, double *waited_ms);
+
 /* Last error message of this handle (never NULL). */
 const char *nb_last_error(nb_handle *h);
 

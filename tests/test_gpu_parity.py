@@ -307,3 +307,33 @@ def test_reupload_smaller_system_into_same_handle(nb, precision):
     ga, gb = nb.get_all_data(a), nb.get_all_data(b)
     np.testing.assert_array_equal(ga["acc"], gb["acc"])
     np.testing.assert_array_equal(ga["pot"], gb["pot"])
+
+
+@pytest.mark.parametrize("law", ["spline", "plummer"])
+def test_uniform_and_mixed_mass_tiles(nb, oracle, law):
+    """Tiles whose sources share one mass take the far-tile loop with the mass
+    applied once per tile; tiles with unequal masses the per-pair loop.  Both
+    match the oracle, and a 1-ulp mass change on one particle (which moves its
+    tile to the per-pair loop) changes no force beyond FP32 round-off."""
+    n, h = 6000, 0.01
+    d = nb.plummer(n, seed=97)
+    d["mass"] = d["mass"].copy()
+    d["mass"][n // 2:] *= np.random.default_rng(5).uniform(0.5, 1.5, n - n // 2)
+    olaw = oracle.LAW_SPLINE_G2 if law == "spline" else oracle.LAW_PLUMMER
+    sim = nb.Simulation(d, ForceSofteningTable=[h] * 6, precision="mixed", law=law)
+    nb.compute_force(sim, want_potential=True)
+    g = nb.get_all_data(sim)
+    a_ref, p_ref = oracle.force(d["pos"], d["mass"], d["pos"], h, law=olaw)
+    e = rel_err(g["acc"], a_ref)
+    assert np.median(e) <= 1e-6 and np.quantile(e, 0.99) <= 1e-5
+    assert np.median(np.abs(g["pot"] - p_ref) / np.abs(p_ref)) <= 1e-6
+
+    u = nb.plummer(n, seed=98)
+    v = dict(u, mass=u["mass"].copy())
+    v["mass"][123] = np.nextafter(v["mass"][123], 1.0)
+    ga, gb = [], []
+    for dd, out in ((u, ga), (v, gb)):
+        s = nb.Simulation(dd, ForceSofteningTable=[h] * 6, precision="mixed", law=law)
+        nb.compute_force(s)
+        out.append(nb.get_all_data(s)["acc"])
+    assert rel_err(ga[0], gb[0]).max() <= 1e-6
