@@ -333,13 +333,17 @@ __global__ void __launch_bounds__(kTileJ)
         origin[g] = make_dvec4(ox, oy, oz, (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
         // box half extents for the near test, enlarged the same way
         const float slack = 4.0e-7f * amax;
-        // ext.w: the common source mass when all are equal, else 0
+        // ext.w: the common source mass when all are equal, else 0 (the pair
+        // loops then apply it once per tile)
         double mlo = mred[0][0], mhi = mred[1][0];
         for (int w = 1; w < kTileJ / 32; ++w) {
             mlo = fmin(mlo, mred[0][w]);
             mhi = fmin(mhi, mred[1][w]);
         }
-        const float mu = (mlo == -mhi && mlo > 0.0) ? (float)mlo : 0.0f;
+        // a partial tile stores -m (its padding adds exactly 0 to the
+        // acceleration in the uniform form, not to the potential)
+        const bool full = (t + 1) * kTileJ <= d.n;
+        const float mu = (mlo == -mhi && mlo > 0.0) ? (full ? (float)mlo : -(float)mlo) : 0.0f;
         ext[g] = make_float4(0.5f * ex * (1.0f + 1e-5f) + slack, 0.5f * ey * (1.0f + 1e-5f) + slack,
                              0.5f * ez * (1.0f + 1e-5f) + slack, mu);
     }
@@ -453,7 +457,7 @@ __global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) 
             if (LAW == NB_LAW_SPLINE_G2)
                 near = warp_near<IPT>(f.ext[d.tile_off + t], xr, yr, zr, hh, pidx);
             if (near)
-                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, f.ext[d.tile_off + t].w);
             else
                 pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, f.ext[d.tile_off + t].w);
             __syncwarp();

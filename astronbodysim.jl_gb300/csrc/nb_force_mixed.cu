@@ -84,9 +84,13 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
         lo[k] = a;
         hi[k] = -b;
     }
-    // ext.w: the common mass of the tile's sources when all are equal (the
-    // far-tile loop then applies it once per tile), else 0.
-    const float mu = (lo[3] == hi[3] && lo[3] > 0.0) ? (float)lo[3] : 0.0f;
+    // ext.w: the common mass m of the tile's sources when all are equal (the
+    // pair loops then apply it once per tile), else 0.  A partial tile stores
+    // -m: its far padding adds exactly 0 to the acceleration in that form
+    // (r^-3 underflows) but not to the potential, so the potential loops use
+    // the per-pair masses there.
+    const bool full = ((int64_t)blockIdx.x + 1) * kTileJ <= n;
+    const float mu = (lo[3] == hi[3] && lo[3] > 0.0) ? (full ? (float)lo[3] : -(float)lo[3]) : 0.0f;
     // Every tile holds at least one particle (tiles cover [0, n)).
     const double ox = 0.5 * (lo[0] + hi[0]);
     const double oy = 0.5 * (lo[1] + hi[1]);
@@ -148,7 +152,7 @@ cudaError_t launch_pack(const double* x, const double* y, const double* z, const
 // DEVERR_TIMEOUT and stops, and the CTA drains its copies before exiting.
 // ---------------------------------------------------------------------------
 template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 : 1) k_force_mixed(Sources32 src, Targets tg, double G,
+__global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && !POT) ? (IPT == 2 ? 8 : (IPT == 1 ? 6 : 1)) : 1) k_force_mixed(Sources32 src, Targets tg, double G,
                                                        uint32_t* __restrict__ err) {
     constexpr int kWarpsPerCta = BLOCK / 32;
     __shared__ __align__(128) float4 buf[kStages * kTileJ];
@@ -248,7 +252,7 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && IPT == 2 && !POT) ? 8 
         bool near = false;
         if (LAW == NB_LAW_SPLINE_G2) near = warp_near<IPT>(src.ext[t_lo + t], xr, yr, zr, hh, pidx);
         if (near)
-            pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+            pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, src.ext[t_lo + t].w);
         else
             pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, src.ext[t_lo + t].w);
 

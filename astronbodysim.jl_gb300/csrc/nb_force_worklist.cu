@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kWBlock, (ACC && !POT) ? 8 : 1) k_force_workli
         if (LAW == NB_LAW_SPLINE_G2)
             near = warp_near<IPT>(w.ext[cur.tile_off + cur.t], xr, yr, zr, hh, pidx);
         if (near)
-            pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap);
+            pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, w.ext[cur.tile_off + cur.t].w);
         else
             pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, w.ext[cur.tile_off + cur.t].w);
 

@@ -70,7 +70,9 @@ __device__ __forceinline__ bool warp_near(const float4 e, const float* xr, const
 // Branch-free loop for far tiles.  UNI: every source of the tile has the same
 // mass mu (flagged by the pack in ext.w), which is then applied once to the
 // tile's partial sums instead of once per pair (one FP32 operation less per
-// interaction).
+// interaction).  Zero-mass padding (at 1e18) then adds r^-3 = 0 exactly to
+// the acceleration (the product underflows) but 1e-18 per slot to the
+// potential, so partial tiles take this form only without the potential.
 template <int LAW, bool ACC, bool POT, int IPT, bool UNI = false>
 __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, const float* xr,
                                                const float* yr, const float* zr, const float* h2,
@@ -147,71 +149,99 @@ template <int LAW, bool ACC, bool POT, int IPT>
 __device__ __forceinline__ void pair_loop_far(const float4* __restrict__ b, const float* xr,
                                               const float* yr, const float* zr, const float* h2,
                                               float* ax, float* ay, float* az, float* ap, float mu) {
-    if (mu > 0.0f)
-        pair_loop_fast<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, h2, ax, ay, az, ap, mu);
+    // mu < 0: uniform but partial tile (usable for the acceleration only)
+    const float m = POT ? mu : fabsf(mu);
+    if (m > 0.0f)
+        pair_loop_fast<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, h2, ax, ay, az, ap, m);
     else
         pair_loop_fast<LAW, ACC, POT, IPT, false>(b, xr, yr, zr, h2, ax, ay, az, ap);
 }
 
-template <int LAW, bool ACC, bool POT, int IPT>
-__device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, const float* xr,
-                                                  const float* yr, const float* zr,
-                                                  const float* hh, const float* h2, float* ax,
-                                                  float* ay, float* az, float* ap) {
+template <int LAW, bool ACC, bool POT, int IPT, bool UNI>
+__device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict__ b, const float* xr,
+                                                       const float* yr, const float* zr,
+                                                       const float* hh, const float* h2, float* ax,
+                                                       float* ay, float* az, float* ap, float mu) {
     // Two passes over the tile.  Pass 1 is the packed FP32x2 loop of
-    // pair_loop_fast with the Newtonian factor of every r < h half set to zero
-    // by a select (so the self pair, r = 0, adds nothing), and a per-thread
-    // flag of whether such a half occurred.  Pass 2 runs only when a lane of
-    // the warp saw one: it walks the tile again and adds the spline terms of
-    // the r < h pairs.
+    // pair_loop_fast (uniform-mass form and split sums included) with the
+    // Newtonian factor of every r < h half set to zero by a select (so the
+    // self pair, r = 0, adds nothing); a 16-bit mask records which blocks of 8
+    // source pairs held such a half.  Pass 2 revisits only the blocks that
+    // some lane of the warp flagged and adds the spline terms of their r < h
+    // pairs.
+    constexpr int NA = (IPT == 1) ? 2 : 1;
     float2 nx[IPT], ny[IPT], nz[IPT];
-    float2 sx[IPT], sy[IPT], sz[IPT], sp[IPT];
-    bool seen[IPT];
+    float2 sx[NA][IPT], sy[NA][IPT], sz[NA][IPT], sp[NA][IPT];
+    uint32_t blk = 0;  // bit q: a r < h half among source pairs 8q .. 8q + 7
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
         nx[k] = make_float2(-xr[k], -xr[k]);
         ny[k] = make_float2(-yr[k], -yr[k]);
         nz[k] = make_float2(-zr[k], -zr[k]);
-        sx[k] = sy[k] = sz[k] = sp[k] = make_float2(0.0f, 0.0f);
-        seen[k] = false;
-    }
-#pragma unroll 4
-    for (int p = 0; p < kTileJ / 2; ++p) {
-        const float4 A = b[2 * p];
-        const float4 B = b[2 * p + 1];
-        const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
-        const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
 #pragma unroll
-        for (int k = 0; k < IPT; ++k) {
-            const float2 dx = __fadd2_rn(qx, nx[k]);
-            const float2 dy = __fadd2_rn(qy, ny[k]);
-            const float2 dz = __fadd2_rn(qz, nz[k]);
-            const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-            const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-            float2 mp = __fmul2_rn(qm, rinv);
-            float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
-            const bool cx = r2.x < h2[k], cy = r2.y < h2[k];
-            seen[k] |= cx | cy;
-            mr3.x = cx ? 0.0f : mr3.x;
-            mr3.y = cy ? 0.0f : mr3.y;
-            if (ACC) {
-                sx[k] = __ffma2_rn(dx, mr3, sx[k]);
-                sy[k] = __ffma2_rn(dy, mr3, sy[k]);
-                sz[k] = __ffma2_rn(dz, mr3, sz[k]);
-            }
-            if (POT) {
-                mp.x = cx ? 0.0f : mp.x;
-                mp.y = cy ? 0.0f : mp.y;
-                sp[k] = __fadd2_rn(sp[k], mp);
+        for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll (4 / NA)
+    for (int p = 0; p < kTileJ / 2; p += NA) {
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+            const float4 A = b[2 * (p + u)];
+            const float4 B = b[2 * (p + u) + 1];
+            const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+            const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                const float2 dx = __fadd2_rn(qx, nx[k]);
+                const float2 dy = __fadd2_rn(qy, ny[k]);
+                const float2 dz = __fadd2_rn(qz, nz[k]);
+                const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+                float2 mp = UNI ? rinv : __fmul2_rn(qm, rinv);
+                float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
+                const bool cx = r2.x < h2[k], cy = r2.y < h2[k];
+                blk |= (uint32_t)(cx | cy) << ((p + u) >> 3);
+                mr3.x = cx ? 0.0f : mr3.x;
+                mr3.y = cy ? 0.0f : mr3.y;
+                if (ACC) {
+                    sx[u][k] = __ffma2_rn(dx, mr3, sx[u][k]);
+                    sy[u][k] = __ffma2_rn(dy, mr3, sy[u][k]);
+                    sz[u][k] = __ffma2_rn(dz, mr3, sz[u][k]);
+                }
+                if (POT) {
+                    mp.x = cx ? 0.0f : mp.x;
+                    mp.y = cy ? 0.0f : mp.y;
+                    sp[u][k] = __fadd2_rn(sp[u][k], mp);
+                }
             }
         }
     }
-    bool any = false;
+    // Fold the split sums (and the common mass) into one set.
+    float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
 #pragma unroll
-    for (int k = 0; k < IPT; ++k) any |= seen[k];
-    if (__any_sync(0xffffffffu, any)) {
+    for (int k = 0; k < IPT; ++k) {
+        tx[k] = sx[0][k];
+        ty[k] = sy[0][k];
+        tz[k] = sz[0][k];
+        tp[k] = sp[0][k];
+#pragma unroll
+        for (int u = 1; u < NA; ++u) {
+            tx[k] = __fadd2_rn(tx[k], sx[u][k]);
+            ty[k] = __fadd2_rn(ty[k], sy[u][k]);
+            tz[k] = __fadd2_rn(tz[k], sz[u][k]);
+            tp[k] = __fadd2_rn(tp[k], sp[u][k]);
+        }
+        if (UNI) {
+            const float2 m2 = make_float2(mu, mu);
+            tx[k] = __fmul2_rn(tx[k], m2);
+            ty[k] = __fmul2_rn(ty[k], m2);
+            tz[k] = __fmul2_rn(tz[k], m2);
+            tp[k] = __fmul2_rn(tp[k], m2);
+        }
+    }
+    for (uint32_t wb = __reduce_or_sync(0xffffffffu, blk); wb != 0u; wb &= wb - 1u) {
+        const int q0 = 8 * (__ffs(wb) - 1);
 #pragma unroll 1
-        for (int p = 0; p < kTileJ / 2; ++p) {
+        for (int p = q0; p < q0 + 8; ++p) {
             const float4 A = b[2 * p];
             const float4 B = b[2 * p + 1];
             const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
@@ -227,18 +257,18 @@ __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, 
                     if (cx) {
                         float mr3, mp;
                         spline_close(r2.x, rsqrt_approx(r2.x), qm.x, hh[k], mr3, mp);
-                        sx[k].x = fmaf(dx.x, mr3, sx[k].x);
-                        sy[k].x = fmaf(dy.x, mr3, sy[k].x);
-                        sz[k].x = fmaf(dz.x, mr3, sz[k].x);
-                        sp[k].x += mp;
+                        tx[k].x = fmaf(dx.x, mr3, tx[k].x);
+                        ty[k].x = fmaf(dy.x, mr3, ty[k].x);
+                        tz[k].x = fmaf(dz.x, mr3, tz[k].x);
+                        tp[k].x += mp;
                     }
                     if (cy) {
                         float mr3, mp;
                         spline_close(r2.y, rsqrt_approx(r2.y), qm.y, hh[k], mr3, mp);
-                        sx[k].y = fmaf(dx.y, mr3, sx[k].y);
-                        sy[k].y = fmaf(dy.y, mr3, sy[k].y);
-                        sz[k].y = fmaf(dz.y, mr3, sz[k].y);
-                        sp[k].y += mp;
+                        tx[k].y = fmaf(dx.y, mr3, tx[k].y);
+                        ty[k].y = fmaf(dy.y, mr3, ty[k].y);
+                        tz[k].y = fmaf(dz.y, mr3, tz[k].y);
+                        tp[k].y += mp;
                     }
                 }
             }
@@ -246,11 +276,24 @@ __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, 
     }
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
-        ax[k] += sx[k].x + sx[k].y;
-        ay[k] += sy[k].x + sy[k].y;
-        az[k] += sz[k].x + sz[k].y;
-        ap[k] += sp[k].x + sp[k].y;
+        ax[k] += tx[k].x + tx[k].y;
+        ay[k] += ty[k].x + ty[k].y;
+        az[k] += tz[k].x + tz[k].y;
+        ap[k] += tp[k].x + tp[k].y;
     }
+}
+
+// Near-tile loop: the uniform-mass form when the pack flagged the tile.
+template <int LAW, bool ACC, bool POT, int IPT>
+__device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, const float* xr,
+                                                  const float* yr, const float* zr,
+                                                  const float* hh, const float* h2, float* ax,
+                                                  float* ay, float* az, float* ap, float mu) {
+    const float m = POT ? mu : fabsf(mu);
+    if (m > 0.0f)
+        pair_loop_checked_impl<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, m);
+    else
+        pair_loop_checked_impl<LAW, ACC, POT, IPT, false>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, 1.0f);
 }
 
 }  // namespace nb
