@@ -58,10 +58,14 @@ class RequestStream:
 
 
 def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_after=False,
-          log=None):
+          log=None, policy="fifo"):
     """Run the request loop for `duration` seconds of wall time.  Arrivals stop
     at `duration`; with drain_after the loop then continues until every arrived
-    request has finished.  Returns latency / throughput statistics."""
+    request has finished.  policy "fifo" hands requests to the engine in
+    arrival order; "sjf" hands the waiting request with the least work
+    (N^2 x steps) first.  Returns latency / throughput statistics."""
+    if policy not in ("fifo", "sjf"):
+        raise ValueError("policy must be 'fifo' or 'sjf'")
     t0 = time.perf_counter()
     pending = []          # arrived, not yet handed to the engine
     inflight = {}         # engine id -> request
@@ -80,6 +84,8 @@ def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_a
             nxt = stream.next()
         st = engine.stats()
         queued = st["queued"]
+        if policy == "sjf" and len(pending) > 1:
+            pending.sort(key=lambda r: float(r["n"]) ** 2 * r["nsteps"])
         while pending and queued < max_engine_queue:
             req = pending.pop(0)
             rid = engine.submit(stream.system(req), req["eps"], stream.dt, req["nsteps"])
@@ -119,6 +125,7 @@ def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_a
         "completed_interactions": done_pairs,
         "backlog_requests": len(pending) + len(inflight),
         "resident_at_end": st1["running"],
+        "policy": policy,
     }
 
 

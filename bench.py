@@ -39,7 +39,8 @@ FLOP_PER_INTERACTION = 20
 L2_FLUSH_BYTES = 256 << 20
 # kernels in one step graph at N = 2^20: clock advance, drift, 2 bounding-box,
 # Morton keys, 8 radix passes x (histogram, 3-kernel scan, scatter), pack,
-# force, kick, clock end
+# force, kick, clock end; plus the join of a j-split force (or the fix-up of
+# the work-list force)
 STEP_KERNELS = 49
 
 
@@ -379,7 +380,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
-            "gpu_launches": STEP_KERNELS * args.steps,
+            "gpu_launches": (STEP_KERNELS + (1 if tuned[2] > 1 or tuned[0] == -1 else 0)) * args.steps,
             "clocks": clocks,
             "accuracy": acc_stats,
             "batch": batch,
@@ -548,6 +549,7 @@ def run_serve(args):
     eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
                     max_steps_per_call=args.serve_chunk, law=args.law)
     st = nb.serve(eng, stream, args.serve_seconds, chunk_steps=args.serve_chunk,
+                  policy=args.serve_policy, max_engine_queue=args.serve_queue,
                   log=lambda k, t: print("completed %d at %.1f s" % (k, t), file=sys.stderr)
                   if k and k % 100 == 0 else None)
     eng.close()
@@ -582,6 +584,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-particles", type=int, default=1 << 22)
+    ap.add_argument("--serve-policy", default="fifo", choices=["fifo", "sjf"])
+    ap.add_argument("--serve-queue", type=int, default=32)
     ap.add_argument("--mode", default="bench", choices=["bench", "serve", "collision", "tune", "ensemble",
                                                          "plummer4096"])
     ap.add_argument("--n-each", type=int, default=1 << 20)
