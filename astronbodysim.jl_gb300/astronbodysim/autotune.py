@@ -2,7 +2,8 @@
 
 For each particle count it times nb_compute_force (mixed precision) with
 every candidate shape -- the direct grid with (threads per CTA, targets per
-thread) in {128, 256} x {1, 2, 4}, and the persistent work-list kernel -- using
+thread, CTAs sharing an i-block's sources) over {128, 256} x {1, 2, 4} x
+{1, 2, 4}, and the persistent work-list kernel -- using
 CUDA events on the handle's stream, and records the fastest in a JSON table
 (tuning_gb300.json next to this file, or a path given by the caller).
 Simulation(tuning=...) looks the table up by the nearest particle count of the
@@ -26,6 +27,7 @@ CANDIDATES = [
     {"block": 256, "i_per_thread": 1, "j_split": 1},
     {"block": 256, "i_per_thread": 2, "j_split": 1},
     {"block": 128, "i_per_thread": 1, "j_split": 2},
+    {"block": 128, "i_per_thread": 1, "j_split": 4},
     {"block": 128, "i_per_thread": 2, "j_split": 2},
     {"block": -1, "i_per_thread": 0, "j_split": 1},  # persistent work list
 ]

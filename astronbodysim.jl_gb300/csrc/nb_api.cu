@@ -56,6 +56,7 @@ struct nb_handle {
     float* partial = nullptr;
     size_t partial_bytes = 0;
     int jsplit = 1;
+    int jalloc = 1;             // j-split the arena's partial buffer holds
     float* jpartial = nullptr;  // j-split partials (arena)
     int64_t jstride = 0;
     std::string err;
@@ -64,6 +65,10 @@ struct nb_handle {
 namespace {
 
 constexpr int kTileJ = 256;
+constexpr int64_t kAutoDirectMin = int64_t(1) << 17;  // built-in rule: direct grid from here
+
+// j-split of the built-in launch rule for n particles.
+int auto_jsplit(int64_t n) { return n >= kAutoDirectMin ? 2 : 1; }
 
 int fail(nb_handle* h, int code, const char* fmt, ...) {
     if (h) {
@@ -206,15 +211,18 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     if (e != cudaSuccess) return e;
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
-    // Measured on GB300 (Plummer, spline): the direct grid with one target per
-    // thread is fastest from N = 2^19 up; below, the evenly split work list
+    // Built-in choice (the autotuner's result on GB300, Plummer, both laws):
+    // from N = 2^17 up the direct grid with one target per thread and each
+    // i-block's tiles split over 2 CTAs; below, the evenly split work list
     // avoids the partial last wave of the direct grid.
     bool use_wl = h->worklist;
     int blk = h->block, ipt = h->ipt;
+    int js = h->jsplit;
     if (h->auto_cfg) {
-        use_wl = h->n < (int64_t(1) << 19);
+        use_wl = h->n < kAutoDirectMin;
         blk = 128;
         ipt = 1;
+        js = auto_jsplit(h->n);
     }
     if (particles && use_wl) {
         if (active_only) {
@@ -267,8 +275,8 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
         }
     }
     nb::Sources32 src{h->pack, h->origin, h->ext, h->ntiles, kTileJ};
-    if (particles && h->jsplit > 1) {
-        src.jsplit = h->jsplit;
+    if (particles && js > 1 && js <= h->jalloc) {
+        src.jsplit = js;
         src.partial = h->jpartial;
         src.pstride = h->jstride;
     }
@@ -319,7 +327,8 @@ cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
 }
 
 int ensure_capacity(nb_handle* h, int64_t n) {
-    if (n <= h->cap && h->arena) return NB_OK;
+    const int js_need = h->auto_cfg ? auto_jsplit(n) : h->jsplit;
+    if (n <= h->cap && h->arena && js_need <= h->jalloc) return NB_OK;
     drop_graph(h);
     if (h->arena) {
         cudaFree(h->arena);
@@ -345,7 +354,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     size_t o_perm = take(sizeof(int32_t) * (size_t)n);
     // j-split partials: jsplit x 8 floats per target slot (slots padded to 1024)
     const int64_t jstride = (n + 1023) / 1024 * 1024;
-    size_t o_jp = take(h->jsplit > 1 ? sizeof(float) * 8 * (size_t)h->jsplit * jstride : 0);
+    size_t o_jp = take(js_need > 1 ? sizeof(float) * 8 * (size_t)js_need * jstride : 0);
     size_t o_acts = take(sizeof(uint32_t) * (size_t)nb::active_scratch_words(n));
     size_t o_sort = take(nb::sort_scratch_bytes(n));
     size_t o_pack = take(sizeof(float4) * (size_t)npad);
@@ -374,7 +383,8 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->ti_end = (int64_t*)(b + o_te);
     h->active = (int32_t*)(b + o_act);
     h->perm = (int32_t*)(b + o_perm);
-    h->jpartial = h->jsplit > 1 ? (float*)(b + o_jp) : nullptr;
+    h->jpartial = js_need > 1 ? (float*)(b + o_jp) : nullptr;
+    h->jalloc = js_need;
     h->jstride = jstride;
     h->act_scratch = (uint32_t*)(b + o_acts);
     h->sort_scratch = (void*)(b + o_sort);
@@ -1006,15 +1016,10 @@ int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
     cudaStream_t s = h->stream;
     NB_CK(cudaStreamSynchronize(s));
     drop_graph(h);
-    const int old_js = h->jsplit;
     h->p = p;
     h->tc = make_timecfg(p);
     apply_tuning(h, p);
-    if (h->jsplit != old_js && h->arena) {  // the arena layout depends on j_split
-        NB_CK(cudaFree(h->arena));
-        h->arena = nullptr;
-        h->cap = 0;
-    }
+    // ensure_capacity re-lays the arena out when the j-split needs more room
     if (n > 0) {
         rc = ensure_capacity(h, n);
         if (rc) return rc;

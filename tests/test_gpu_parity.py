@@ -337,3 +337,33 @@ def test_uniform_and_mixed_mass_tiles(nb, oracle, law):
         nb.compute_force(s)
         out.append(nb.get_all_data(s)["acc"])
     assert rel_err(ga[0], gb[0]).max() <= 1e-6
+
+
+def test_builtin_rule_at_large_n_matches_explicit_shape_and_oracle(nb, oracle):
+    """Without a tuning table the library picks its shape by N: from 2^17 the
+    direct grid with the j-split.  It agrees with an explicit unsplit shape and
+    the oracle, repeats bit for bit, and survives re-uploads across the
+    threshold (the arena is re-laid out for the split partials)."""
+    n, h = (1 << 17) + 5, 0.01
+    d = nb.plummer(n, seed=101)
+    a = nb.Simulation(d, ForceSofteningTable=[h] * 6, precision="mixed")
+    b = nb.Simulation(d, ForceSofteningTable=[h] * 6, precision="mixed", block=128, i_per_thread=1)
+    nb.compute_force(a)
+    ga = nb.get_all_data(a)["acc"]
+    nb.compute_force(a)
+    np.testing.assert_array_equal(ga, nb.get_all_data(a)["acc"])
+    nb.compute_force(b)
+    assert rel_err(ga, nb.get_all_data(b)["acc"]).max() <= 1e-6
+    sub = np.arange(0, n, 512)
+    a_ref, _ = oracle.force(d["pos"], d["mass"], d["pos"][sub], h)
+    e = rel_err(ga[sub], a_ref)
+    assert np.median(e) <= 1e-6 and np.quantile(e, 0.99) <= 1e-5
+    small = nb.plummer(5000, seed=102)
+    a.upload(small)
+    nb.compute_force(a)
+    c = nb.Simulation(small, ForceSofteningTable=[h] * 6, precision="mixed")
+    nb.compute_force(c)
+    np.testing.assert_array_equal(nb.get_all_data(a)["acc"], nb.get_all_data(c)["acc"])
+    a.upload(d)
+    nb.compute_force(a)
+    np.testing.assert_array_equal(nb.get_all_data(a)["acc"], ga)
