@@ -65,10 +65,9 @@ struct nb_handle {
 namespace {
 
 constexpr int kTileJ = 256;
-constexpr int64_t kAutoDirectMin = int64_t(1) << 17;  // built-in rule: direct grid from here
-
-// j-split of the built-in launch rule for n particles.
-int auto_jsplit(int64_t n) { return n >= kAutoDirectMin ? 2 : 1; }
+// j-split of the built-in launch rule (the autotuner's choice on GB300 for
+// every N from 2^12 to 2^20, both laws).
+constexpr int kAutoJsplit = 4;
 
 int fail(nb_handle* h, int code, const char* fmt, ...) {
     if (h) {
@@ -211,18 +210,19 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     if (e != cudaSuccess) return e;
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
-    // Built-in choice (the autotuner's result on GB300, Plummer, both laws):
-    // from N = 2^17 up the direct grid with one target per thread and each
-    // i-block's tiles split over 2 CTAs; below, the evenly split work list
-    // avoids the partial last wave of the direct grid.
+    // Built-in choice (the autotuner's result on GB300, Plummer, both laws,
+    // N = 2^12 .. 2^20): the direct grid with one target per thread and each
+    // i-block's tiles split over 4 CTAs, whose compensated partials are joined
+    // in order.  The split keeps the grid several waves deep at small N, where
+    // the work list was used before.
     bool use_wl = h->worklist;
     int blk = h->block, ipt = h->ipt;
     int js = h->jsplit;
     if (h->auto_cfg) {
-        use_wl = h->n < kAutoDirectMin;
+        use_wl = false;
         blk = 128;
         ipt = 1;
-        js = auto_jsplit(h->n);
+        js = kAutoJsplit;
     }
     if (particles && use_wl) {
         if (active_only) {
@@ -327,7 +327,7 @@ cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
 }
 
 int ensure_capacity(nb_handle* h, int64_t n) {
-    const int js_need = h->auto_cfg ? auto_jsplit(n) : h->jsplit;
+    const int js_need = h->auto_cfg ? kAutoJsplit : h->jsplit;
     if (n <= h->cap && h->arena && js_need <= h->jalloc) return NB_OK;
     drop_graph(h);
     if (h->arena) {

@@ -340,10 +340,10 @@ def test_uniform_and_mixed_mass_tiles(nb, oracle, law):
 
 
 def test_builtin_rule_at_large_n_matches_explicit_shape_and_oracle(nb, oracle):
-    """Without a tuning table the library picks its shape by N: from 2^17 the
-    direct grid with the j-split.  It agrees with an explicit unsplit shape and
-    the oracle, repeats bit for bit, and survives re-uploads across the
-    threshold (the arena is re-laid out for the split partials)."""
+    """Without a tuning table the library uses the direct grid with the
+    j-split.  It agrees with an explicit unsplit shape and the oracle, repeats
+    bit for bit, and survives re-uploads of smaller and larger systems into the
+    same handle."""
     n, h = (1 << 17) + 5, 0.01
     d = nb.plummer(n, seed=101)
     a = nb.Simulation(d, ForceSofteningTable=[h] * 6, precision="mixed")
