@@ -114,12 +114,14 @@ __device__ __forceinline__ uint64_t spread3_21(uint64_t v) {
     return v;
 }
 
-// 63-bit Morton key of a point in the box bbox (lo = bbox[0..2], hi = -bbox[3..5]).
-__device__ __forceinline__ uint64_t morton_key(double px, double py, double pz,
-                                               const double* bbox) {
+__global__ void k_morton(const double* __restrict__ x, const double* __restrict__ y,
+                         const double* __restrict__ z, int64_t n, const double* __restrict__ bbox,
+                         uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    const int64_t i = (int64_t)blockIdx.x * kSortThreads + threadIdx.x;
+    if (i >= n) return;
     const double lo[3] = {bbox[0], bbox[1], bbox[2]};
     const double hi[3] = {-bbox[3], -bbox[4], -bbox[5]};
-    const double p[3] = {px, py, pz};
+    const double p[3] = {x[i], y[i], z[i]};
     uint64_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -128,89 +130,8 @@ __device__ __forceinline__ uint64_t morton_key(double px, double py, double pz,
         f = fmin(fmax(f, 0.0), 1.0);
         q[k] = (uint64_t)(f * 2097151.0);
     }
-    return spread3_21(q[0]) | (spread3_21(q[1]) << 1) | (spread3_21(q[2]) << 2);
-}
-
-__global__ void k_morton(const double* __restrict__ x, const double* __restrict__ y,
-                         const double* __restrict__ z, int64_t n, const double* __restrict__ bbox,
-                         uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
-    const int64_t i = (int64_t)blockIdx.x * kSortThreads + threadIdx.x;
-    if (i >= n) return;
-    keys[i] = morton_key(x[i], y[i], z[i], bbox);
+    keys[i] = spread3_21(q[0]) | (spread3_21(q[1]) << 1) | (spread3_21(q[2]) << 2);
     vals[i] = (int32_t)i;
-}
-
-// Whole Morton sort of a small system in one CTA: bounding box, keys and a
-// bitonic sort of (key, index) pairs in shared memory.  Ordering by (key,
-// index) gives exactly the permutation of the stable radix sort, in one
-// launch instead of 43 (the radix path is launch-bound at this size).
-constexpr int kSmallSortMax = 4096;  // 4096 x 12 B = 48 KB of shared memory
-constexpr int kSmallSortThreads = 1024;
-
-__global__ void __launch_bounds__(kSmallSortThreads)
-    k_morton_sort_small(const double* __restrict__ x, const double* __restrict__ y,
-                        const double* __restrict__ z, int n, int np2, int32_t* __restrict__ perm) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint64_t* key = reinterpret_cast<uint64_t*>(smem);
-    int32_t* idx = reinterpret_cast<int32_t*>(smem + sizeof(uint64_t) * np2);
-    double* red = reinterpret_cast<double*>(smem);  // bounding-box partials, before the keys
-    const int tid = threadIdx.x;
-    double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
-    for (int i = tid; i < n; i += kSmallSortThreads) {
-        const double a = x[i], b = y[i], c = z[i];
-        v[0] = fmin(v[0], a);
-        v[1] = fmin(v[1], b);
-        v[2] = fmin(v[2], c);
-        v[3] = fmin(v[3], -a);
-        v[4] = fmin(v[4], -b);
-        v[5] = fmin(v[5], -c);
-    }
-#pragma unroll
-    for (int k = 0; k < 6; ++k)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
-    constexpr int kW = kSmallSortThreads / 32;
-    if ((tid & 31) == 0)
-#pragma unroll
-        for (int k = 0; k < 6; ++k) red[k * kW + (tid >> 5)] = v[k];
-    __syncthreads();
-    // every thread reduces the partials itself (no static shared memory: the
-    // keys and indices may take the whole 48 KB), then the partials' space is
-    // reused for the keys
-    double box[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        double r = red[k * kW];
-        for (int w = 1; w < kW; ++w) r = fmin(r, red[k * kW + w]);
-        box[k] = r;
-    }
-    __syncthreads();
-    for (int i = tid; i < np2; i += kSmallSortThreads) {
-        key[i] = i < n ? morton_key(x[i], y[i], z[i], box) : ~0ull;
-        idx[i] = i;
-    }
-    __syncthreads();
-    for (int k = 2; k <= np2; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < np2; i += kSmallSortThreads) {
-                const int ixj = i ^ j;
-                if (ixj > i) {
-                    const uint64_t ka = key[i], kb = key[ixj];
-                    const int32_t ia = idx[i], ib = idx[ixj];
-                    const bool a_gt_b = ka > kb || (ka == kb && ia > ib);
-                    const bool up = (i & k) == 0;
-                    if (a_gt_b == up) {
-                        key[i] = kb;
-                        key[ixj] = ka;
-                        idx[i] = ib;
-                        idx[ixj] = ia;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    for (int i = tid; i < n; i += kSmallSortThreads) perm[i] = idx[i];
 }
 
 __global__ void __launch_bounds__(kSortThreads)
@@ -421,15 +342,6 @@ cudaError_t launch_sort_keys(void* scratch, int64_t n, int32_t* vals, int passes
 cudaError_t launch_morton_sort(const double* x, const double* y, const double* z, int64_t n,
                                void* scratch, int32_t* perm, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    if (n <= kSmallSortMax) {
-        int np2 = 1;
-        while (np2 < n) np2 <<= 1;
-        size_t smem = (size_t)np2 * (sizeof(uint64_t) + sizeof(int32_t));
-        const size_t red_bytes = sizeof(double) * 6 * (kSmallSortThreads / 32);
-        if (smem < red_bytes) smem = red_bytes;
-        k_morton_sort_small<<<1, kSmallSortThreads, smem, s>>>(x, y, z, (int)n, np2, perm);
-        return cudaGetLastError();
-    }
     SortScratch sc = carve(scratch, n);
     int64_t gb = (n + kSortThreads - 1) / kSortThreads;
     const int bb = (int)(gb < kBboxBlocks ? gb : kBboxBlocks);
