@@ -242,12 +242,12 @@ __global__ void __launch_bounds__(kTileJ)
                  const double* __restrict__ z, const double* __restrict__ m,
                  float4* __restrict__ pack, dvec4* __restrict__ origin, float4* __restrict__ ext) {
     // The tile's bounding box is reduced in FP32 relative to the tile's first
-    // particle c (FP64); the tile origin c + float offset is exact in FP64 and
-    // the sources are then re-expressed relative to it in FP64.  Everything
-    // depends on this tile's particles only.
+    // particle c (FP64); the tile origin is c + float offset, and the sources
+    // are re-expressed relative to it from their FP64 offsets to c.  The
+    // common-mass test compares bit patterns.  FP64 work (slow on this GPU) is
+    // kept to the offsets.  Everything depends on this tile's particles only.
     __shared__ float red[6][kTileJ / 32];
-    __shared__ double mred[2][kTileJ / 32];
-    __shared__ double cref[3];
+    __shared__ double cref[4];
     const int32_t g = blockIdx.x;
     const int32_t r = tile_rank[g];
     const SysDesc& d = sys[r];
@@ -267,10 +267,13 @@ __global__ void __launch_bounds__(kTileJ)
         cref[0] = px;
         cref[1] = py;
         cref[2] = pz;
+        cref[3] = pm;
     }
     __syncthreads();
-    const double cx = cref[0], cy = cref[1], cz = cref[2];
-    const float fx = (float)(px - cx), fy = (float)(py - cy), fz = (float)(pz - cz);
+    const double cx = cref[0], cy = cref[1], cz = cref[2], m0 = cref[3];
+    const double dx = px - cx, dy = py - cy, dz = pz - cz;
+    const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+    const bool same_mass = !valid || __double_as_longlong(pm) == __double_as_longlong(m0);
     float v[6];
     v[0] = valid ? fx : 3e38f;
     v[1] = valid ? fy : 3e38f;
@@ -282,19 +285,12 @@ __global__ void __launch_bounds__(kTileJ)
     for (int k = 0; k < 6; ++k)
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
-    double mm[2] = {valid ? pm : 1e300, valid ? -pm : 1e300};  // smallest / largest mass
-#pragma unroll
-    for (int k = 0; k < 2; ++k)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mm[k] = fmin(mm[k], __shfl_xor_sync(0xffffffffu, mm[k], o));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
-        mred[0][warp] = mm[0];
-        mred[1][warp] = mm[1];
     }
-    __syncthreads();
+    const bool uniform = __syncthreads_and(same_mass) && m0 > 0.0;
     float lo[3], hi[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -308,12 +304,12 @@ __global__ void __launch_bounds__(kTileJ)
         hi[k] = -b;
     }
     const float oxf = 0.5f * (lo[0] + hi[0]), oyf = 0.5f * (lo[1] + hi[1]), ozf = 0.5f * (lo[2] + hi[2]);
-    const double ox = cx + (double)oxf, oy = cy + (double)oyf, oz = cz + (double)ozf;
+    const double oxd = (double)oxf, oyd = (double)oyf, ozd = (double)ozf;
     float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
     if (valid) {
-        qx = (float)(px - ox);
-        qy = (float)(py - oy);
-        qz = (float)(pz - oz);
+        qx = (float)(dx - oxd);
+        qy = (float)(dy - oyd);
+        qz = (float)(dz - ozd);
         qm = (float)pm;
     }
     float* base = reinterpret_cast<float*>(pack + (int64_t)g * kTileJ);
@@ -330,20 +326,15 @@ __global__ void __launch_bounds__(kTileJ)
         const float amax = fmaxf(fmaxf(fabsf(lo[0]), fabsf(hi[0])),
                                  fmaxf(fmaxf(fabsf(lo[1]), fabsf(hi[1])),
                                        fmaxf(fabsf(lo[2]), fabsf(hi[2]))));
-        origin[g] = make_dvec4(ox, oy, oz, (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
+        origin[g] = make_dvec4(cx + oxd, cy + oyd, cz + ozd, (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
         // box half extents for the near test, enlarged the same way
         const float slack = 4.0e-7f * amax;
         // ext.w: the common source mass when all are equal, else 0 (the pair
         // loops then apply it once per tile)
-        double mlo = mred[0][0], mhi = mred[1][0];
-        for (int w = 1; w < kTileJ / 32; ++w) {
-            mlo = fmin(mlo, mred[0][w]);
-            mhi = fmin(mhi, mred[1][w]);
-        }
         // a partial tile stores -m (its padding adds exactly 0 to the
         // acceleration in the uniform form, not to the potential)
         const bool full = (t + 1) * kTileJ <= d.n;
-        const float mu = (mlo == -mhi && mlo > 0.0) ? (full ? (float)mlo : -(float)mlo) : 0.0f;
+        const float mu = uniform ? (full ? (float)m0 : -(float)m0) : 0.0f;
         ext[g] = make_float4(0.5f * ex * (1.0f + 1e-5f) + slack, 0.5f * ey * (1.0f + 1e-5f) + slack,
                              0.5f * ez * (1.0f + 1e-5f) + slack, mu);
     }
