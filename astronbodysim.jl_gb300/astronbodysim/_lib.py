@@ -155,6 +155,7 @@ SIGNATURES = {
     "nb_diagnostics": (ctypes.c_int, [_h, ctypes.c_int, ctypes.POINTER(nb_diag)]),
     "nb_active_count": (ctypes.c_int, [_h, _i64p]),
     "nb_get_counters": (ctypes.c_int, [_h, _i64p, _dp]),
+    "nb_check_sync_point": (ctypes.c_int, [_h, ctypes.POINTER(ctypes.c_int32)]),
     "nb_batch_suspend": (ctypes.c_int, [_h, ctypes.c_int64]),
     "nb_batch_resume": (ctypes.c_int, [_h, ctypes.c_int64]),
     "nb_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, _dp]),

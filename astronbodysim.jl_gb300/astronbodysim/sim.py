@@ -300,6 +300,14 @@ def loadrestart(filename, device=None):
     return sim
 
 
+def check_sync_point(sim):
+    """check_sync_point (src/directsumgpu/timestep.jl:116-118): True when every
+    particle's Ti_endstep is past the last min_endstep (a full sync point)."""
+    v = ctypes.c_int32()
+    sim._ck(sim._lib.nb_check_sync_point(sim.handle, ctypes.byref(v)))
+    return bool(v.value)
+
+
 def get_all_data(sim):
     """src/base/Config.jl:1228-1230 (download to host)."""
     return sim.download()

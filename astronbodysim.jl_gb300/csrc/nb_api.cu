@@ -826,6 +826,23 @@ int nb_find_min_endstep(nb_handle* h, int64_t* min_endstep) {
     return sync_and_check(h);
 }
 
+int nb_check_sync_point(nb_handle* h, int32_t* sync) {
+    if (!h || !sync) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    // the diagnostics' 8-double output slot serves as the counter
+    unsigned long long* count = reinterpret_cast<unsigned long long*>(h->diag_out);
+    NB_CK(nb::launch_sync_count(h->ti_end, h->n, h->clk, count, h->stream));
+    unsigned long long c = 0;
+    NB_CK(cudaMemcpyAsync(&c, count, sizeof c, cudaMemcpyDeviceToHost, h->stream));
+    rc = sync_and_check(h);
+    if (rc) return rc;
+    *sync = c == (unsigned long long)h->n ? 1 : 0;
+    return NB_OK;
+}
+
 int nb_drift_to_int(nb_handle* h, int64_t t_int) {
     if (!h) return NB_ERR_INVALID_ARG;
     int rc = use_device(h);

@@ -274,6 +274,37 @@ cudaError_t launch_min_endstep(const int64_t* ti_end, int64_t n, int64_t time_ba
     return cudaGetLastError();
 }
 
+// check_sync_point_local (src/base/Timestep.jl:146-157): counts the particles
+// with Ti_endstep > min_endstep (the value of the last find_min_endstep); all
+// of them are past it exactly at a full synchronisation point.
+__global__ void k_sync_count(const int64_t* __restrict__ ti_end, int64_t n, const Clock* clk,
+                             unsigned long long* count) {
+    __shared__ unsigned long long red[kBlock / 32];
+    const int64_t m = clk->min_endstep;
+    unsigned long long c = 0;
+    for (int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * kBlock)
+        c += ti_end[i] > m ? 1ull : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kBlock / 32; ++w) c += red[w];
+        atomicAdd(count, c);
+    }
+}
+
+cudaError_t launch_sync_count(const int64_t* ti_end, int64_t n, const Clock* clk,
+                              unsigned long long* count, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || n <= 0) return e;
+    int64_t g = (n + kBlock - 1) / kBlock;
+    if (g > 1216) g = 1216;
+    k_sync_count<<<(unsigned)g, kBlock, 0, s>>>(ti_end, n, clk, count);
+    return cudaGetLastError();
+}
+
 // Clock advance before a drift (single thread).
 //   mode 0: adaptive, to min_endstep       (src/directsum/timestep.jl:1-20)
 //   mode 1: adaptive, to t_int_arg

@@ -240,6 +240,10 @@ cudaError_t launch_half_kick(double* vx, double* vy, double* vz, const double* a
                              const double* ay, const double* az, const int64_t* ti_beg,
                              const int64_t* ti_end, int64_t n, TimeCfg cfg, int forward,
                              cudaStream_t s);
+// Particles with Ti_endstep > clk->min_endstep, counted into *count.
+cudaError_t launch_sync_count(const int64_t* ti_end, int64_t n, const Clock* clk,
+                              unsigned long long* count, cudaStream_t s);
+
 // Force post-processing (background field, then Milgrom MOND); see nb_params.
 struct PostCfg {
     int32_t bg_kind;

@@ -177,6 +177,14 @@ function AstroNbodySim.find_min_endstep(sim::Simulation, ::Gravity, ::GPU)
     return v[]
 end
 
+# src/directsumgpu/timestep.jl:116-118 (check_sync_point_local on the device data)
+function AstroNbodySim.check_sync_point(sim::Simulation, ::Gravity, ::GPU)
+    h = handle(sim)
+    v = Ref{Int32}(0)
+    check(h, ccall((:nb_check_sync_point, libnb), Cint, (Ptr{Cvoid}, Ref{Int32}), h.ptr, v))
+    return sim.outputinfo.syncflag = v[] != 0
+end
+
 # src/directsumgpu/timestep.jl:76-91: the host keeps TimeInfo, the device follows
 function AstroNbodySim.drift_particles_kernel(sim::Simulation, ::AdaptiveTimestep, ::Gravity, ::GPU)
     h = handle(sim)

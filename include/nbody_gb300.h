@@ -200,6 +200,12 @@ int nb_diagnostics(nb_handle *h, int with_potential, nb_diag *out);
  * (active targets x all sources per step). */
 int nb_get_counters(nb_handle *h, int64_t *steps, double *interactions);
 
+/* check_sync_point for GPU (src/directsumgpu/timestep.jl:116-118,
+ * src/base/Timestep.jl:146-157): *sync = 1 when every particle's Ti_endstep
+ * is past the min_endstep of the last nb_find_min_endstep (or of the last
+ * adaptive nb_step), i.e. the system is at a full synchronisation point. */
+int nb_check_sync_point(nb_handle *h, int32_t *sync);
+
 /* Number of particles active at the current time (Ti_endstep == t_int). */
 int nb_active_count(nb_handle *h, int64_t *count);
 

@@ -223,3 +223,29 @@ def test_collision_adaptive_mixed_vs_fp64(nb):
     em = (m1["K"] + m1["W"]) / (m0["K"] + m0["W"]) - 1
     assert abs(em - ef) < 1e-5, (em, ef)
     np.testing.assert_allclose(mg["pos"], fg["pos"], rtol=0, atol=1e-4)
+
+
+def test_check_sync_point_follows_the_time_line(nb, oracle):
+    """check_sync_point is true exactly after the steps at which every particle
+    was active (all Ti_endstep past the step's min_endstep); FP64 run against
+    the oracle's time line."""
+    d = nb.plummer(600, seed=13)
+    h, T1 = 0.01, 0.05
+    o = oracle.OracleSim(d["pos"], d["vel"], d["mass"], soft=[h] * 6, time_end=T1, max_step=1e-2)
+    o.run_begin()
+    sim = nb.Simulation(d, ForceSofteningTable=[h] * 6, TimeEnd=T1, MaxStep=1e-2, precision="fp64")
+    nb.compute_force(sim)
+    nb.init_timesteps(sim)
+    nb.leapfrog_half_kick(sim, +1)
+    seen = {True: 0, False: 0}
+    for _ in range(40):
+        m = o.find_min_endstep()
+        o.step(1)
+        nb.step(sim, 1)
+        flag = nb.check_sync_point(sim)
+        assert flag == bool(np.all(o.ti_end > m))
+        assert flag == bool(np.all(nb.get_all_data(sim)["ti_endstep"] > m))
+        seen[flag] += 1
+        if o.t_int >= 1 << 30:
+            break
+    assert seen[True] > 0 and seen[False] > 0
