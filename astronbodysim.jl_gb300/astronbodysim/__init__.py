@@ -9,7 +9,7 @@ from .engine import Engine
 from .serve import RequestStream, ensemble_systems, serve
 from .ics import collision, hernquist, plummer
 from .gadget2 import internal_G, read_gadget2, write_gadget2, write_snapshot
-from .sim import (DirectSum, GPU, MOND1983Milgrom, Newton, PointMassField, PseudoNewtonianField,
+from .sim import (DirectSum, Euler, GPU, Leapfrog, MOND1983Milgrom, Newton, PointMassField, PseudoNewtonianField,
                   Simulation, active_count, advance_and_find_timestep,
                   compute_force, compute_potential, const_step_count, counters, diagnostics,
                   drift_particles_adaptive_timestep, drift_particles_const_timestep,
@@ -19,7 +19,7 @@ from .sim import (DirectSum, GPU, MOND1983Milgrom, Newton, PointMassField, Pseud
                   total_potential)
 
 __all__ = [
-    "MOND1983Milgrom", "Newton", "PointMassField", "PseudoNewtonianField",
+    "Euler", "Leapfrog", "MOND1983Milgrom", "Newton", "PointMassField", "PseudoNewtonianField",
     "read_gadget2", "write_gadget2", "write_snapshot", "internal_G",
     "Engine", "RequestStream", "ensemble_systems", "serve", "NbodyError", "load", "plummer", "hernquist", "collision", "DirectSum", "GPU", "Simulation",
     "active_count", "counters", "advance_and_find_timestep", "compute_force", "compute_potential",

@@ -41,6 +41,16 @@ class Newton:
     """Gravity model trait (src/base/Traits.jl): plain Newtonian forces."""
 
 
+class Leapfrog:
+    """Time integration trait: KDK leapfrog, i.e. the step loop between a
+    forward and a backward half kick (src/run.jl:85-87, 171-173)."""
+
+
+class Euler:
+    """Time integration trait: the same step loop without the half kicks
+    (src/run.jl:85-87 and 171-173 apply them only for Leapfrog)."""
+
+
 class MOND1983Milgrom:
     """Gravity model trait: Newtonian forces scaled by the Milgrom (1983)
     interpolation nu(|a| / ACC0, MOND_nuIndex) (src/mond/milgrom1983.jl)."""
@@ -88,7 +98,7 @@ class Simulation:
                  TimeEnd=0.1, TimeBase=1 << 30, ErrTolTimestep=0.025, MinStep=1.0e-8,
                  MaxStep=float("inf"), law="spline", precision="mixed", criterion="ref",
                  device=None, block=0, i_per_thread=0, j_split=0, tuning=None, bgforce=None,
-                 GravityModel=None, ACC0=0.0, MOND_nuIndex=2.0):
+                 GravityModel=None, ACC0=0.0, MOND_nuIndex=2.0, TimeIntegrationAlgorithm=None):
         self._lib = L.load()
         p = L.nb_params()
         self._lib.nb_default_params(ctypes.byref(p))
@@ -139,6 +149,11 @@ class Simulation:
         p.j_split = int(j_split)
         self.tuned_shape = (int(block), int(i_per_thread), int(j_split))
         self.params = p
+        alg = TimeIntegrationAlgorithm
+        self.euler = alg is Euler or isinstance(alg, Euler) or alg == "Euler"
+        if alg is not None and not self.euler and not (alg is Leapfrog or isinstance(alg, Leapfrog)
+                                                       or alg == "Leapfrog"):
+            raise ValueError("TimeIntegrationAlgorithm must be Leapfrog or Euler")
         self.G = float(G)
         self.softening = [float(s) for s in soft]
         self.TimeBegin = float(TimeBegin)
@@ -282,9 +297,11 @@ def saverestart(sim, filename):
         f.write(sim.checkpoint())
 
 
-def loadrestart(filename, device=None):
+def loadrestart(filename, device=None, TimeIntegrationAlgorithm=None):
     """loadrestart (src/restart.jl:129-139): a new Simulation on `device`
-    (default: the saved one) holding the saved state."""
+    (default: the saved one) holding the saved state.  The time-integration
+    algorithm is a property of the host loop, not of the image: pass Euler
+    again for a run that used it."""
     with open(filename, "rb") as f:
         image = f.read()
     p = L.nb_params.from_buffer_copy(image, _CKPT_PARAMS_OFFSET)
@@ -295,7 +312,8 @@ def loadrestart(filename, device=None):
                      MinStep=p.min_step, MaxStep=p.max_step, law=inv(LAWS, p.law),
                      precision=inv(PRECISIONS, p.precision), criterion=inv(CRITERIA, p.criterion),
                      device=p.device if device is None else device, block=p.block,
-                     i_per_thread=p.i_per_thread, j_split=p.j_split)
+                     i_per_thread=p.i_per_thread, j_split=p.j_split,
+                     TimeIntegrationAlgorithm=TimeIntegrationAlgorithm)
     sim.restore(image)
     return sim
 
@@ -412,8 +430,13 @@ def const_step_count(begin, end, dt):
 def run(sim, nsteps=None):
     """src/run.jl:46-184 without output/logging: warm-up force, init timesteps,
     forward half kick, the step loop until TimeEnd (or exactly `nsteps` steps),
-    backward half kick."""
-    sim._ck(sim._lib.nb_run_begin(sim.handle))
+    backward half kick.  With TimeIntegrationAlgorithm Euler the half kicks
+    are left out, as the reference does."""
+    if getattr(sim, "euler", False):
+        compute_force(sim)
+        init_timesteps(sim)
+    else:
+        sim._ck(sim._lib.nb_run_begin(sim.handle))
     if nsteps is not None:
         step(sim, nsteps)
     elif not sim.adaptive:
@@ -424,7 +447,8 @@ def run(sim, nsteps=None):
             _, tf = sim.time()
             if tf >= sim.TimeEnd:
                 break
-    leapfrog_half_kick(sim, -1)
+    if not getattr(sim, "euler", False):
+        leapfrog_half_kick(sim, -1)
 
 
 def diagnostics(sim, with_potential=True):

@@ -249,3 +249,40 @@ def test_check_sync_point_follows_the_time_line(nb, oracle):
         if o.t_int >= 1 << 30:
             break
     assert seen[True] > 0 and seen[False] > 0
+
+
+@pytest.mark.parametrize("adaptive", [False, True])
+def test_euler_time_integration_matches_oracle(nb, oracle, adaptive):
+    """TimeIntegrationAlgorithm = Euler: the step loop without the half kicks
+    (src/run.jl:85-87, 171-173), FP64 against the oracle driven the same way;
+    the circular-orbit setting of test/Local-Timestep.jl:760-790 (two massless
+    particles around a point-mass background field)."""
+    GM, R = 1.0, 1.0
+    v = np.sqrt(GM / R)
+    d = {"pos": np.array([[R, 0, 0], [-R, 0, 0]], float),
+         "vel": np.array([[0, v, 0], [0, -v, 0]], float), "mass": np.zeros(2)}
+    T = 0.5
+    kw = dict(ForceSofteningTable=[1e-4] * 6, TimeEnd=T, precision="fp64",
+              bgforce=nb.PointMassField(GM), TimeIntegrationAlgorithm=nb.Euler)
+    okw = dict(soft=[1e-4] * 6, time_end=T, bg_kind=1, bg_gm=GM)
+    if adaptive:
+        kw.update(MaxStep=1e-2)
+        okw.update(max_step=1e-2)
+    else:
+        kw.update(TimeStep=1e-3)
+        okw.update(dt=1e-3)
+    sim = nb.Simulation(d, **kw)
+    nb.run(sim, nsteps=200)
+    o = oracle.OracleSim(d["pos"], d["vel"], d["mass"], **okw)
+    o.compute_force()
+    o.init_timesteps()
+    o.step(200)
+    g = nb.get_all_data(sim)
+    np.testing.assert_allclose(g["pos"], o.pos, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(g["vel"], o.vel, rtol=0, atol=1e-12)
+
+
+def test_unknown_time_integration_algorithm(nb):
+    with pytest.raises(ValueError):
+        nb.Simulation(nb.plummer(16, seed=1), ForceSofteningTable=[0.01] * 6,
+                      TimeIntegrationAlgorithm="RK4")
