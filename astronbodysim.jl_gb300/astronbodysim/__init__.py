@@ -15,6 +15,7 @@ from .sim import (DirectSum, Euler, GPU, Leapfrog, MOND1983Milgrom, Newton, Poin
                   drift_particles_adaptive_timestep, drift_particles_const_timestep,
                   find_min_endstep, force_and_potential_at_points, get_all_data,
                   check_sync_point, init_timesteps, leapfrog_half_kick, loadrestart, run, saverestart, set_softlen, step,
+                  step_until_output,
                   total_angular_momentum, total_energy, total_kinetic, total_momentum,
                   total_potential)
 
@@ -25,6 +26,6 @@ __all__ = [
     "active_count", "counters", "advance_and_find_timestep", "compute_force", "compute_potential",
     "const_step_count", "diagnostics", "drift_particles_adaptive_timestep",
     "drift_particles_const_timestep", "find_min_endstep", "force_and_potential_at_points",
-    "get_all_data", "check_sync_point", "saverestart", "loadrestart", "init_timesteps", "leapfrog_half_kick", "run", "set_softlen", "step",
+    "get_all_data", "check_sync_point", "saverestart", "loadrestart", "init_timesteps", "leapfrog_half_kick", "run", "set_softlen", "step", "step_until_output",
     "total_angular_momentum", "total_energy", "total_kinetic", "total_momentum", "total_potential",
 ]

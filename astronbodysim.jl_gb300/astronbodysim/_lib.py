@@ -27,6 +27,8 @@ NB_PREC_MIXED = 1
 NB_CRIT_REF = 0
 NB_CRIT_ETA_SQRT_EPS = 1
 NB_FORCE_POT = 1
+NB_ALG_LEAPFROG = 0
+NB_ALG_EULER = 1
 
 _ERRNAMES = {
     NB_ERR_INVALID_ARG: "NB_ERR_INVALID_ARG", NB_ERR_OOM: "NB_ERR_OOM", NB_ERR_CUDA: "NB_ERR_CUDA",
@@ -64,7 +66,7 @@ class nb_params(ctypes.Structure):
         ("i_per_thread", ctypes.c_int32),
         ("block", ctypes.c_int32),
         ("j_split", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("algorithm", ctypes.c_int32),
         ("bg_kind", ctypes.c_int32),
         ("mond", ctypes.c_int32),
         ("bg_gm", ctypes.c_double),
@@ -151,6 +153,10 @@ SIGNATURES = {
     "nb_drift_to_float": (ctypes.c_int, [_h, ctypes.c_double]),
     "nb_step": (ctypes.c_int, [_h, ctypes.c_int64]),
     "nb_run_begin": (ctypes.c_int, [_h]),
+    "nb_run_end": (ctypes.c_int, [_h]),
+    "nb_set_snapshot_interval": (ctypes.c_int, [_h, ctypes.c_double]),
+    "nb_step_until_output": (ctypes.c_int, [_h, ctypes.c_int64, _i64p, _i32p]),
+    "nb_get_output_time": (ctypes.c_int, [_h, _i64p, _dp, _i32p, _i64p]),
     "nb_get_time": (ctypes.c_int, [_h, _i64p, _dp]),
     "nb_diagnostics": (ctypes.c_int, [_h, ctypes.c_int, ctypes.POINTER(nb_diag)]),
     "nb_active_count": (ctypes.c_int, [_h, _i64p]),

@@ -9,6 +9,8 @@ Names, argument meaning and error behaviour follow the reference:
   compute_potential(sim)                          src/base/Potential.jl:21-24
   init_timesteps, leapfrog_half_kick, advance_and_find_timestep, find_min_endstep,
   step, run                                       src/directsumgpu/timestep.jl, src/run.jl
+  TimeBetweenSnapshots + OutputFunc: snapshots at output times inside steps
+  (find_next_sync_point_and_drift)               src/base/Timestep.jl:197-245
   total_kinetic / total_potential / total_energy / total_momentum /
   total_angular_momentum                          src/base/Energy.jl
 Errors raised by the reference's CPU path (error("Timestep < MinStep ...")) come
@@ -98,7 +100,8 @@ class Simulation:
                  TimeEnd=0.1, TimeBase=1 << 30, ErrTolTimestep=0.025, MinStep=1.0e-8,
                  MaxStep=float("inf"), law="spline", precision="mixed", criterion="ref",
                  device=None, block=0, i_per_thread=0, j_split=0, tuning=None, bgforce=None,
-                 GravityModel=None, ACC0=0.0, MOND_nuIndex=2.0, TimeIntegrationAlgorithm=None):
+                 GravityModel=None, ACC0=0.0, MOND_nuIndex=2.0, TimeIntegrationAlgorithm=None,
+                 TimeBetweenSnapshots=None, OutputFunc=None):
         self._lib = L.load()
         p = L.nb_params()
         self._lib.nb_default_params(ctypes.byref(p))
@@ -154,6 +157,9 @@ class Simulation:
         if alg is not None and not self.euler and not (alg is Leapfrog or isinstance(alg, Leapfrog)
                                                        or alg == "Leapfrog"):
             raise ValueError("TimeIntegrationAlgorithm must be Leapfrog or Euler")
+        # the library applies (or skips) the run's half kicks and keeps the
+        # choice in checkpoint images
+        p.algorithm = L.NB_ALG_EULER if self.euler else L.NB_ALG_LEAPFROG
         self.G = float(G)
         self.softening = [float(s) for s in soft]
         self.TimeBegin = float(TimeBegin)
@@ -168,6 +174,13 @@ class Simulation:
             raise L.NbodyError(rc, "nb_create failed (check parameters / device)")
         self.handle = h
         self.n = 0
+        # sim.config.output.func: called with the simulation at every output
+        # time (the initial conditions and each time the time line reaches
+        # TimeBegin + k * TimeBetweenSnapshots)
+        self.output_func = OutputFunc
+        self.TimeBetweenSnapshots = 0.0
+        if TimeBetweenSnapshots:
+            self.set_snapshot_interval(TimeBetweenSnapshots)
         if data is not None:
             self.upload(data)
 
@@ -231,6 +244,7 @@ class Simulation:
         arrays = 11 * 8 * n + (4 * n + 7) // 8 * 8 + 16 * n
         hdr = len(image) - arrays
         self.params = p
+        self.euler = p.algorithm == L.NB_ALG_EULER
         self.G = p.G
         self.softening = list(p.softening)
         self.TimeBegin, self.TimeEnd = p.time_begin, p.time_end
@@ -242,6 +256,21 @@ class Simulation:
         self.mass = np.frombuffer(image, dtype=np.float64, count=n, offset=hdr + 10 * 8 * n).copy()
         self.collection = np.frombuffer(image, dtype=np.int32, count=n,
                                         offset=hdr + 11 * 8 * n).copy()
+
+    def set_snapshot_interval(self, between):
+        """TimeBetweenSnapshots (src/base/Config.jl:392-394, 436-439): output
+        times TimeBegin + k * between; 0 turns output stops off."""
+        self._ck(self._lib.nb_set_snapshot_interval(self.handle, float(between)))
+        self.TimeBetweenSnapshots = float(between)
+
+    def output_state(self):
+        """(next output time on the integer line, next output time, stopped
+        at an output, output stops so far)."""
+        ni, nf = ctypes.c_int64(), ctypes.c_double()
+        at, k = ctypes.c_int32(), ctypes.c_int64()
+        self._ck(self._lib.nb_get_output_time(self.handle, ctypes.byref(ni), ctypes.byref(nf),
+                                              ctypes.byref(at), ctypes.byref(k)))
+        return ni.value, nf.value, bool(at.value), k.value
 
     def set_stream(self, stream_ptr):
         self._ck(self._lib.nb_set_stream(self.handle, ctypes.c_void_p(stream_ptr)))
@@ -297,14 +326,16 @@ def saverestart(sim, filename):
         f.write(sim.checkpoint())
 
 
-def loadrestart(filename, device=None, TimeIntegrationAlgorithm=None):
+def loadrestart(filename, device=None, OutputFunc=None):
     """loadrestart (src/restart.jl:129-139): a new Simulation on `device`
-    (default: the saved one) holding the saved state.  The time-integration
-    algorithm is a property of the host loop, not of the image: pass Euler
-    again for a run that used it."""
+    (default: the saved one) holding the saved state, with the saved
+    time-integration algorithm (Leapfrog or Euler) and snapshot schedule, as
+    the reference's restart file keeps the whole SimConfig."""
     with open(filename, "rb") as f:
         image = f.read()
     p = L.nb_params.from_buffer_copy(image, _CKPT_PARAMS_OFFSET)
+    between = float(np.frombuffer(image, dtype=np.float64, count=1,
+                                  offset=_CKPT_PARAMS_OFFSET + ctypes.sizeof(L.nb_params))[0])
     inv = lambda d, v: next(k for k, x in d.items() if x == v)  # noqa: E731
     sim = Simulation(None, G=p.G, ForceSofteningTable=list(p.softening),
                      TimeStep=p.dt if not p.adaptive else 0.0, TimeBegin=p.time_begin,
@@ -313,8 +344,10 @@ def loadrestart(filename, device=None, TimeIntegrationAlgorithm=None):
                      precision=inv(PRECISIONS, p.precision), criterion=inv(CRITERIA, p.criterion),
                      device=p.device if device is None else device, block=p.block,
                      i_per_thread=p.i_per_thread, j_split=p.j_split,
-                     TimeIntegrationAlgorithm=TimeIntegrationAlgorithm)
+                     TimeIntegrationAlgorithm=Euler if p.algorithm == L.NB_ALG_EULER else Leapfrog,
+                     OutputFunc=OutputFunc)
     sim.restore(image)
+    sim.TimeBetweenSnapshots = between
     return sim
 
 
@@ -397,8 +430,32 @@ def drift_particles_const_timestep(sim, next_float):
 
 
 def step(sim, nsteps=1):
-    """step(sim, DirectSum, GPU) repeated nsteps times (CUDA-graph replay)."""
-    sim._ck(sim._lib.nb_step(sim.handle, int(nsteps)))
+    """step(sim, DirectSum, GPU) repeated nsteps times (CUDA-graph replay).
+    With TimeBetweenSnapshots set, each step splits its drift at the output
+    times inside it and calls sim.output_func there, as
+    find_next_sync_point_and_drift does (src/base/Timestep.jl:197-245)."""
+    nsteps = int(nsteps)
+    if not sim.TimeBetweenSnapshots or sim.output_func is None:
+        sim._ck(sim._lib.nb_step(sim.handle, nsteps))
+        return
+    done = 0
+    k, at = ctypes.c_int64(), ctypes.c_int32()
+    while done < nsteps:
+        sim._ck(sim._lib.nb_step_until_output(sim.handle, nsteps - done, ctypes.byref(k),
+                                              ctypes.byref(at)))
+        done += k.value
+        if at.value:
+            sim.output_func(sim)
+
+
+def step_until_output(sim, max_steps):
+    """At most max_steps steps, stopping at the first output time reached:
+    returns (steps completed, True if stopped at an output time).  The next
+    call finishes the interrupted step."""
+    k, at = ctypes.c_int64(), ctypes.c_int32()
+    sim._ck(sim._lib.nb_step_until_output(sim.handle, int(max_steps), ctypes.byref(k),
+                                          ctypes.byref(at)))
+    return k.value, bool(at.value)
 
 
 def counters(sim):
@@ -428,15 +485,15 @@ def const_step_count(begin, end, dt):
 
 
 def run(sim, nsteps=None):
-    """src/run.jl:46-184 without output/logging: warm-up force, init timesteps,
-    forward half kick, the step loop until TimeEnd (or exactly `nsteps` steps),
-    backward half kick.  With TimeIntegrationAlgorithm Euler the half kicks
-    are left out, as the reference does."""
-    if getattr(sim, "euler", False):
-        compute_force(sim)
-        init_timesteps(sim)
-    else:
-        sim._ck(sim._lib.nb_run_begin(sim.handle))
+    """src/run.jl:46-184 without logging: warm-up force, init timesteps,
+    forward half kick, the initial snapshot (sim.output_func, if any), the step
+    loop until TimeEnd (or exactly `nsteps` steps) with snapshots at the output
+    times, backward half kick.  With TimeIntegrationAlgorithm Euler the half
+    kicks are left out, as the reference does (the library applies the choice
+    in nb_run_begin / nb_run_end)."""
+    sim._ck(sim._lib.nb_run_begin(sim.handle))
+    if sim.output_func is not None:
+        sim.output_func(sim)  # src/run.jl:90
     if nsteps is not None:
         step(sim, nsteps)
     elif not sim.adaptive:
@@ -447,8 +504,7 @@ def run(sim, nsteps=None):
             _, tf = sim.time()
             if tf >= sim.TimeEnd:
                 break
-    if not getattr(sim, "euler", False):
-        leapfrog_half_kick(sim, -1)
+    sim._ck(sim._lib.nb_run_end(sim.handle))
 
 
 def diagnostics(sim, with_potential=True):

@@ -45,6 +45,8 @@ struct nb_handle {
     void* probe = nullptr;
     size_t probe_bytes = 0;
     cudaGraphExec_t step_exec = nullptr;
+    cudaGraphExec_t out_exec = nullptr;  // step graph that stops at output times
+    double between = 0.0;                 // BetweenSnapshots (0: no output stops)
     int block = 128;
     int ipt = 2;
     bool worklist = false;     // persistent work-list kernel forced (block == -1)
@@ -91,7 +93,7 @@ int fail(nb_handle* h, int code, const char* fmt, ...) {
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-TimeCfg make_timecfg(const nb_params& p) {
+TimeCfg make_timecfg(const nb_params& p, double between) {
     TimeCfg c{};
     c.adaptive = p.adaptive;
     c.criterion = p.criterion;
@@ -103,6 +105,22 @@ TimeCfg make_timecfg(const nb_params& p) {
     c.time_interval = (p.time_end - p.time_begin) / (double)p.time_base;
     c.time_begin = p.time_begin;
     for (int k = 0; k < 6; ++k) c.soft[k] = p.softening[k];
+    // BetweenSnapshotsInt = floor(BetweenSnapshots / TimeInterval) for adaptive
+    // steps, 0 for constant steps (src/base/Config.jl:436-439)
+    c.between_float = between;
+    c.between_int = p.adaptive ? (int64_t)std::floor(between / c.time_interval) : 0;
+    c.outputs_on = between > 0.0 ? 1 : 0;
+    return c;
+}
+
+// TimeInfo at construction (src/base/Config.jl:742-761): t = Begin, first
+// output at Begin + BetweenSnapshots (integer line: BetweenSnapshotsInt).
+Clock initial_clock(const nb_params& p, const TimeCfg& tc) {
+    Clock c{};
+    c.t_float = p.time_begin;
+    c.last_t_float = p.time_begin;
+    c.next_out_int = tc.between_int;
+    c.next_out_float = p.time_begin + tc.between_float;
     return c;
 }
 
@@ -142,6 +160,8 @@ int check_params(nb_handle* h, const nb_params* p) {
         return fail(h, NB_ERR_INVALID_ARG, "j_split must be 0..4");
     if (p->tile_j != 0 && p->tile_j != kTileJ)
         return fail(h, NB_ERR_INVALID_ARG, "tile_j must be %d", kTileJ);
+    if (p->algorithm != NB_ALG_LEAPFROG && p->algorithm != NB_ALG_EULER)
+        return fail(h, NB_ERR_INVALID_ARG, "algorithm must be NB_ALG_LEAPFROG or NB_ALG_EULER");
     return NB_OK;
 }
 
@@ -149,6 +169,10 @@ void drop_graph(nb_handle* h) {
     if (h->step_exec) {
         cudaGraphExecDestroy(h->step_exec);
         h->step_exec = nullptr;
+    }
+    if (h->out_exec) {
+        cudaGraphExecDestroy(h->out_exec);
+        h->out_exec = nullptr;
     }
 }
 
@@ -326,6 +350,79 @@ cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
     return nb::launch_clock_end_step(h->clk, h->p.adaptive, h->n, s);
 }
 
+// The step graph with snapshot stops (find_next_sync_point_and_drift with
+// outputs, src/base/Timestep.jl:197-245): [min end step] -> plan -> gated
+// drift -> IF(condition){force, post-processing, kick, clock}.  The plan
+// kernel sets the condition, so a replay either completes a step or stops the
+// time line at an output time inside it; the IF body is skipped on the device
+// without a host round trip.
+cudaError_t capture_output_graph(nb_handle* h, cudaGraphExec_t* out) {
+    *out = nullptr;
+    cudaStream_t s = h->own_stream;
+    const bool adaptive = h->p.adaptive != 0;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return e;
+    cudaGraphConditionalHandle cond = 0;
+    e = cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return e;
+    }
+    e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        return e;
+    }
+    cudaGraph_t body = nullptr;
+    if (adaptive) e = nb::launch_min_endstep(h->ti_end, h->n, h->p.time_base, h->clk, s);
+    if (e == cudaSuccess)
+        e = nb::launch_plan_and_drift(h->x, h->y, h->z, h->vx, h->vy, h->vz, h->n, h->tc, h->clk,
+                                      cond, s);
+    if (e == cudaSuccess) {
+        cudaStreamCaptureStatus st;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        e = cudaStreamGetCaptureInfo(s, &st, nullptr, nullptr, &deps, nullptr, &ndeps);
+        if (e == cudaSuccess) {
+            cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+            cp.conditional.handle = cond;
+            cp.conditional.type = cudaGraphCondTypeIf;
+            cp.conditional.size = 1;
+            cudaGraphNode_t node = nullptr;
+            e = cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &cp);
+            if (e == cudaSuccess) {
+                body = cp.conditional.phGraph_out[0];
+                e = cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                                        cudaStreamSetCaptureDependencies);
+            }
+        }
+    }
+    cudaGraph_t g2 = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(s, &g2);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) {
+        // the IF body: the rest of step(sim, DirectSum, GPU)
+        e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            e = enqueue_force(h, particle_targets(h, true, false), s, adaptive);
+            if (e == cudaSuccess) e = enqueue_post(h, s, adaptive);
+            if (e == cudaSuccess)
+                e = nb::launch_kick(h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->type, h->ti_beg,
+                                    h->ti_end, h->n, h->tc, h->clk, s);
+            if (e == cudaSuccess) e = nb::launch_clock_end_step(h->clk, h->p.adaptive, h->n, s);
+            cudaGraph_t b2 = nullptr;
+            e2 = cudaStreamEndCapture(s, &b2);
+            if (e == cudaSuccess) e = e2;
+        }
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) *out = nullptr;
+    return e;
+}
+
 int ensure_capacity(nb_handle* h, int64_t n) {
     const int js_need = h->auto_cfg ? kAutoJsplit : h->jsplit;
     if (n <= h->cap && h->arena && js_need <= h->jalloc) return NB_OK;
@@ -425,7 +522,8 @@ void apply_tuning(nb_handle* h, const nb_params& p) {
 
 // Checkpoint image: this header, then x, y, z, vx, vy, vz, ax, ay, az, pot, m
 // (FP64, n each), type (int32, n, padded to 8 bytes), Ti_begstep, Ti_endstep
-// (int64, n each).
+// (int64, n each).  The parameters carry the time-integration algorithm and
+// the clock the snapshot schedule, so a restored run keeps both.
 struct CkptHeader {
     char magic[8];
     int64_t version;
@@ -434,10 +532,12 @@ struct CkptHeader {
     int64_t params_size;
     int64_t clock_size;
     nb_params p;
+    double between;  // BetweenSnapshots (0: no output stops)
+    double pad;
     Clock clk;
 };
 constexpr char kCkptMagic[8] = {'N', 'B', 'G', 'B', '3', '0', '0', 'C'};
-constexpr int64_t kCkptVersion = 1;
+constexpr int64_t kCkptVersion = 2;
 
 int64_t ckpt_bytes(int64_t n) {
     return (int64_t)sizeof(CkptHeader) + 11 * 8 * n + (int64_t)align_up(4 * (size_t)n, 8) + 16 * n;
@@ -495,7 +595,7 @@ int nb_create(const nb_params* p, nb_handle** out) {
         return NB_ERR_CUDA;
     }
     h->p = *p;
-    h->tc = make_timecfg(*p);
+    h->tc = make_timecfg(*p, 0.0);
     h->dev = p->device;
     if (cudaSetDevice(h->dev) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -505,9 +605,7 @@ int nb_create(const nb_params* p, nb_handle** out) {
         return NB_ERR_CUDA;
     }
     h->stream = h->own_stream;
-    Clock c{};
-    c.t_float = p->time_begin;
-    c.last_t_float = p->time_begin;
+    Clock c = initial_clock(*p, h->tc);
     cudaMemcpy(h->clk, &c, sizeof c, cudaMemcpyHostToDevice);
     // Work-list force: persistent grid = CTAs per SM x SMs for each variant;
     // the partial-sum scratch is sized for the largest grid.
@@ -616,9 +714,7 @@ int nb_upload(nb_handle* h, int64_t n, const double* x, const double* y, const d
     NB_CK(cudaMemsetAsync(h->pot, 0, d, s));
     NB_CK(cudaMemsetAsync(h->ti_beg, 0, sizeof(int64_t) * (size_t)n, s));
     NB_CK(cudaMemsetAsync(h->ti_end, 0, sizeof(int64_t) * (size_t)n, s));
-    Clock c{};
-    c.t_float = h->p.time_begin;
-    c.last_t_float = h->p.time_begin;
+    Clock c = initial_clock(h->p, h->tc);
     NB_CK(cudaMemcpyAsync(h->clk, &c, sizeof c, cudaMemcpyHostToDevice, s));
     NB_CK(cudaStreamSynchronize(s));
     return upload_sysdesc(h);
@@ -681,7 +777,7 @@ int nb_set_softening(nb_handle* h, const double soft[6]) {
         if (!(soft[k] > 0.0) || !std::isfinite(soft[k]))
             return fail(h, NB_ERR_INVALID_ARG, "softening[%d] must be finite and > 0", k);
     for (int k = 0; k < 6; ++k) h->p.softening[k] = soft[k];
-    h->tc = make_timecfg(h->p);
+    h->tc = make_timecfg(h->p, h->between);
     drop_graph(h);
     if (h->n > 0) {
         int rc = use_device(h);
@@ -861,6 +957,52 @@ int nb_drift_to_float(nb_handle* h, double t_float) {
     return sync_and_check(h);
 }
 
+// Replays of the output-aware step graph until `nsteps` steps are complete;
+// with stop_at_output the call returns at the first output time reached
+// (*at_output = 1), otherwise it continues through output times (the drift
+// is still split there).  *done = complete steps.
+static int step_with_outputs(nb_handle* h, int64_t nsteps, bool stop_at_output, int64_t* done,
+                      int32_t* at_output) {
+    *done = 0;
+    *at_output = 0;
+    if (!h->out_exec) {
+        NB_CK(cudaStreamSynchronize(h->stream));
+        cudaError_t e = capture_output_graph(h, &h->out_exec);
+        if (e != cudaSuccess)
+            return fail(h, NB_ERR_CUDA, "output step graph capture failed: %s", cudaGetErrorString(e));
+    }
+    // Replays after an output stop are no-ops on the device, so the host reads
+    // the clock between chunks instead of after every step.
+    struct {
+        int64_t steps;
+        int32_t at_output;
+    } st;
+    Clock c{};
+    NB_CK(cudaStreamSynchronize(h->stream));
+    NB_CK(cudaMemcpy(&c, h->clk, sizeof c, cudaMemcpyDeviceToHost));
+    const int64_t steps0 = c.steps;
+    st.steps = c.steps;
+    st.at_output = c.at_output;
+    while (st.steps - steps0 < nsteps) {
+        if (st.at_output) {
+            // the host has seen this output: resume the step
+            NB_CK(cudaMemsetAsync(&h->clk->at_output, 0, sizeof(int32_t), h->stream));
+        }
+        int64_t chunk = nsteps - (st.steps - steps0);
+        if (chunk > 32) chunk = 32;
+        for (int64_t k = 0; k < chunk; ++k) NB_CK(cudaGraphLaunch(h->out_exec, h->stream));
+        int rc = sync_and_check(h);
+        if (rc) return rc;
+        NB_CK(cudaMemcpy(&c, h->clk, sizeof c, cudaMemcpyDeviceToHost));
+        st.steps = c.steps;
+        st.at_output = c.at_output;
+        if (st.at_output && stop_at_output) break;
+    }
+    *done = st.steps - steps0;
+    *at_output = st.at_output;
+    return NB_OK;
+}
+
 int nb_step(nb_handle* h, int64_t nsteps) {
     if (!h || nsteps < 0) return fail(h, NB_ERR_INVALID_ARG, "nsteps must be >= 0");
     int rc = use_device(h);
@@ -868,6 +1010,11 @@ int nb_step(nb_handle* h, int64_t nsteps) {
     rc = require_particles(h);
     if (rc) return rc;
     if (nsteps == 0) return NB_OK;
+    if (h->tc.outputs_on) {
+        int64_t done = 0;
+        int32_t at = 0;
+        return step_with_outputs(h, nsteps, false, &done, &at);
+    }
     if (!h->step_exec) {
         // Capture one step on the handle's own (non-default) stream; the graph
         // is then launched on whatever stream the handle currently uses.
@@ -892,12 +1039,80 @@ int nb_step(nb_handle* h, int64_t nsteps) {
     return sync_and_check(h);
 }
 
+int nb_step_until_output(nb_handle* h, int64_t max_steps, int64_t* steps_done,
+                         int32_t* at_output) {
+    if (!h || max_steps < 0 || !steps_done || !at_output)
+        return fail(h, NB_ERR_INVALID_ARG, "max_steps must be >= 0 and the outputs non-NULL");
+    *steps_done = 0;
+    *at_output = 0;
+    int rc = use_device(h);
+    if (rc) return rc;
+    rc = require_particles(h);
+    if (rc) return rc;
+    if (max_steps == 0) return NB_OK;
+    if (!h->tc.outputs_on) {
+        rc = nb_step(h, max_steps);
+        if (rc) return rc;
+        *steps_done = max_steps;
+        return NB_OK;
+    }
+    return step_with_outputs(h, max_steps, true, steps_done, at_output);
+}
+
+int nb_set_snapshot_interval(nb_handle* h, double between) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    if (!(between >= 0.0) || !std::isfinite(between))
+        return fail(h, NB_ERR_INVALID_ARG, "BetweenSnapshots must be finite and >= 0");
+    const TimeCfg tc = make_timecfg(h->p, between);
+    if (tc.outputs_on && h->p.adaptive && tc.between_int <= 0)
+        return fail(h, NB_ERR_INVALID_ARG,
+                    "BetweenSnapshots %.17g is below TimeInterval %.17g: BetweenSnapshotsInt would be 0",
+                    between, tc.time_interval);
+    int rc = use_device(h);
+    if (rc) return rc;
+    Clock c{};
+    NB_CK(cudaStreamSynchronize(h->stream));
+    NB_CK(cudaMemcpy(&c, h->clk, sizeof c, cudaMemcpyDeviceToHost));
+    if (c.mid_step)
+        return fail(h, NB_ERR_STATE, "the time line is stopped at an output time inside a step");
+    drop_graph(h);
+    h->between = between;
+    h->tc = tc;
+    const Clock c0 = initial_clock(h->p, tc);
+    c.next_out_int = c0.next_out_int;
+    c.next_out_float = c0.next_out_float;
+    NB_CK(cudaMemcpy(h->clk, &c, sizeof c, cudaMemcpyHostToDevice));
+    return NB_OK;
+}
+
+int nb_get_output_time(nb_handle* h, int64_t* next_int, double* next_float, int32_t* at_output,
+                       int64_t* outputs) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    int rc = use_device(h);
+    if (rc) return rc;
+    Clock c{};
+    NB_CK(cudaStreamSynchronize(h->stream));
+    NB_CK(cudaMemcpy(&c, h->clk, sizeof c, cudaMemcpyDeviceToHost));
+    if (next_int) *next_int = c.next_out_int;
+    if (next_float) *next_float = c.next_out_float;
+    if (at_output) *at_output = c.at_output;
+    if (outputs) *outputs = c.outputs;
+    return NB_OK;
+}
+
 int nb_run_begin(nb_handle* h) {
     int rc = nb_compute_force(h, 0);
     if (rc) return rc;
     rc = nb_init_timesteps(h);
     if (rc) return rc;
+    if (h->p.algorithm == NB_ALG_EULER) return NB_OK;
     return nb_half_kick(h, +1);
+}
+
+int nb_run_end(nb_handle* h) {
+    if (!h) return NB_ERR_INVALID_ARG;
+    if (h->p.algorithm == NB_ALG_EULER) return NB_OK;
+    return nb_half_kick(h, -1);
 }
 
 int nb_get_time(nb_handle* h, int64_t* t_int, double* t_float) {
@@ -986,6 +1201,7 @@ int nb_checkpoint_save(nb_handle* h, void* buf, int64_t bytes) {
     hd.params_size = (int64_t)sizeof(nb_params);
     hd.clock_size = (int64_t)sizeof(Clock);
     hd.p = h->p;
+    hd.between = h->between;
     NB_CK(cudaMemcpy(&hd.clk, h->clk, sizeof(Clock), cudaMemcpyDeviceToHost));
     char* b = static_cast<char*>(buf);
     std::memcpy(b, &hd, sizeof hd);
@@ -1023,6 +1239,8 @@ int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
     p.device = h->dev;  // the image moves to this handle's device
     int rc = check_params(h, &p);
     if (rc) return rc;
+    if (!(hd.between >= 0.0) || !std::isfinite(hd.between))
+        return fail(h, NB_ERR_INVALID_ARG, "checkpoint image has a bad snapshot interval");
     const char* b = static_cast<const char*>(buf);
     const int32_t* type = reinterpret_cast<const int32_t*>(b + sizeof hd + 11 * 8 * (size_t)n);
     for (int64_t i = 0; i < n; ++i)
@@ -1034,7 +1252,8 @@ int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
     NB_CK(cudaStreamSynchronize(s));
     drop_graph(h);
     h->p = p;
-    h->tc = make_timecfg(p);
+    h->between = hd.between;
+    h->tc = make_timecfg(p, hd.between);
     apply_tuning(h, p);
     // ensure_capacity re-lays the arena out when the j-split needs more room
     if (n > 0) {

@@ -346,6 +346,77 @@ cudaError_t launch_drift(double* x, double* y, double* z, const double* vx, cons
     return cudaGetLastError();
 }
 
+// find_next_sync_point_and_drift with snapshots (src/base/Timestep.jl:197-215
+// constant, :224-245 adaptive), one event per graph replay (single thread).
+// The step ends at t_float + dt (constant) or at min_endstep (adaptive); while
+// the next output time is at or before that end, the reference drifts to the
+// output time, writes the snapshot and moves the output time on by
+// BetweenSnapshots.  Here the clock advances to that output time, the
+// condition of the force/kick branch is 0, and at_output stops further
+// replays until the host has written the snapshot and cleared it; the next
+// replay continues the same step (mid_step) towards the next output or the
+// step's end.  The clock arithmetic is the reference's: t_float = Begin +
+// t_int * TimeInterval and drift interval (t_int - last) * TimeInterval for
+// adaptive steps, drift interval t_float - last_t_float for constant steps.
+__global__ void k_clock_plan(Clock* clk, TimeCfg c, cudaGraphConditionalHandle cond) {
+    if (clk->at_output) {
+        clk->drift_skip = 1;
+        cudaGraphSetConditional(cond, 0u);
+        return;
+    }
+    clk->drift_skip = 0;
+    bool stop;
+    if (c.adaptive) {
+        const int64_t target = clk->mid_step ? clk->step_target_int : clk->min_endstep;
+        stop = c.outputs_on && clk->next_out_int <= target;
+        const int64_t next = stop ? clk->next_out_int : target;
+        if (stop) {
+            clk->step_target_int = target;
+            clk->next_out_int += c.between_int;
+        }
+        clk->last_t_int = clk->t_int;
+        clk->t_int = next;
+        clk->t_float = c.time_begin + (double)clk->t_int * c.time_interval;
+        clk->dt_drift = (double)(clk->t_int - clk->last_t_int) * c.time_interval;
+    } else {
+        const double target = clk->mid_step ? clk->step_target_float : clk->t_float + c.dt;
+        stop = c.outputs_on && clk->next_out_float <= target;
+        const double next = stop ? clk->next_out_float : target;
+        if (stop) {
+            clk->step_target_float = target;
+            clk->next_out_float += c.between_float;
+        }
+        clk->last_t_float = clk->t_float;
+        clk->t_float = next;
+        clk->dt_drift = clk->t_float - clk->last_t_float;
+    }
+    clk->mid_step = stop ? 1 : 0;
+    clk->at_output = stop ? 1 : 0;
+    if (stop) clk->outputs += 1;
+    cudaGraphSetConditional(cond, stop ? 0u : 1u);
+}
+
+// k_drift of a replay planned by k_clock_plan (no-op when drift_skip is set).
+__global__ void k_drift_gated(double* __restrict__ x, double* __restrict__ y,
+                              double* __restrict__ z, const double* __restrict__ vx,
+                              const double* __restrict__ vy, const double* __restrict__ vz,
+                              int64_t n, const Clock* __restrict__ clk) {
+    const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+    if (i >= n || clk->drift_skip) return;
+    const double dt = clk->dt_drift;
+    x[i] = x[i] + vx[i] * dt;
+    y[i] = y[i] + vy[i] * dt;
+    z[i] = z[i] + vz[i] * dt;
+}
+
+cudaError_t launch_plan_and_drift(double* x, double* y, double* z, const double* vx,
+                                  const double* vy, const double* vz, int64_t n, TimeCfg cfg,
+                                  Clock* clk, cudaGraphConditionalHandle cond, cudaStream_t s) {
+    k_clock_plan<<<1, 1, 0, s>>>(clk, cfg, cond);
+    if (n > 0) k_drift_gated<<<grid_for(n), kBlock, 0, s>>>(x, y, z, vx, vy, vz, n, clk);
+    return cudaGetLastError();
+}
+
 __global__ void k_clock_end_step(Clock* clk, int adaptive, int64_t n) {
     if (!adaptive) clk->last_t_float = clk->t_float;  // src/run.jl:164
     const double targets = adaptive ? (double)clk->n_active : (double)n;

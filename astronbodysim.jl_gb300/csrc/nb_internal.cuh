@@ -37,6 +37,19 @@ struct Clock {
     uint32_t err;           // DEVERR_* bits
     double interactions;    // sum over steps of (targets x sources)
     int64_t steps;          // steps taken through the step graph
+    // Snapshot schedule (TimeInfo.next_output_time_int / _float,
+    // src/base/Config.jl:732-733, 749-750) and the state of a step that
+    // stopped at an output time inside it (find_next_sync_point_and_drift,
+    // src/base/Timestep.jl:197-245).
+    int64_t next_out_int;     // next output time on the integer time line
+    double next_out_float;    // next output time (constant steps)
+    int64_t step_target_int;  // end of the step being split (adaptive)
+    double step_target_float; // end of the step being split (constant)
+    int32_t mid_step;         // 1: positions sit at an output time inside a step
+    int32_t at_output;        // 1: stopped at an output, waiting for the host
+    int32_t drift_skip;       // 1: the gated drift of this replay does nothing
+    int32_t pad;
+    int64_t outputs;          // output stops so far
 };
 
 // Timestep configuration passed by value.
@@ -51,6 +64,12 @@ struct TimeCfg {
     double time_interval;
     double time_begin;
     double soft[6];
+    // Snapshot interval (TimeConfig.BetweenSnapshots / BetweenSnapshotsInt,
+    // src/base/Config.jl:392-394, 436-439); outputs_on 0 = no output stops.
+    int32_t outputs_on;
+    int32_t pad;
+    double between_float;
+    int64_t between_int;
 };
 
 // Targets of a force evaluation.  Target slot t maps to particle idx[t]
@@ -269,6 +288,14 @@ cudaError_t launch_drift(double* x, double* y, double* z, const double* vx, cons
                          const double* vz, int64_t n, TimeCfg cfg, Clock* clk, int mode,
                          int64_t t_int_arg, double t_float_arg, cudaStream_t s);
 cudaError_t launch_clock_end_step(Clock* clk, int adaptive, int64_t n, cudaStream_t s);
+// One event of find_next_sync_point_and_drift (src/base/Timestep.jl:197-245):
+// the clock advances to the next output time when it falls inside the step
+// (setting at_output and the graph condition to 0), else to the step's end
+// (condition 1: force and kick follow); then the gated drift.  A replay that
+// finds at_output still set does nothing.
+cudaError_t launch_plan_and_drift(double* x, double* y, double* z, const double* vx,
+                                  const double* vy, const double* vz, int64_t n, TimeCfg cfg,
+                                  Clock* clk, cudaGraphConditionalHandle cond, cudaStream_t s);
 cudaError_t launch_diag(const double* x, const double* y, const double* z, const double* vx,
                         const double* vy, const double* vz, const double* m, const double* pot,
                         int64_t n, double* scratch, int64_t scratch_blocks, double* out8,

@@ -42,6 +42,10 @@ extern "C" {
 #define NB_CRIT_REF 0          /* dt = sqrt(2 eta h / |a|), src/base/Timestep.jl:3 */
 #define NB_CRIT_ETA_SQRT_EPS 1 /* dt = eta sqrt(h / |a|) */
 
+/* TimeIntegrationAlgorithm (src/base/Config.jl:398, src/run.jl:85-87, 171-173) */
+#define NB_ALG_LEAPFROG 0 /* run begins with a +1/2 kick and ends with a -1/2 kick */
+#define NB_ALG_EULER 1    /* the same step loop without the half kicks */
+
 /* flags of nb_compute_force */
 #define NB_FORCE_POT 1 /* also write the potential per unit mass */
 
@@ -70,7 +74,8 @@ typedef struct nb_params {
                              -1 = persistent work-list kernel; 0 (with i_per_thread 0) = auto */
     int32_t j_split;      /* tuning override: CTAs sharing one i-block's sources in the direct
                              grid (1..4; 0 = 1) */
-    int32_t reserved;
+    int32_t algorithm;    /* NB_ALG_LEAPFROG (default) or NB_ALG_EULER: whether nb_run_begin /
+                             nb_run_end apply the half kicks; kept in checkpoint images */
     /* Force post-processing, applied by nb_compute_force and nb_step to the
      * particles that received a force (postprocessing_force,
      * src/directsumgpu/gravity.jl:64-79; CPU src/base/PostProcessing/Force.jl:33-47):
@@ -186,8 +191,48 @@ int nb_drift_to_float(nb_handle *h, double t_float);
  * captured once in a CUDA graph and replayed; the time line lives on the device. */
 int nb_step(nb_handle *h, int64_t nsteps);
 
-/* src/run.jl:76-87: force, init_timesteps, forward half kick. */
+/* src/run.jl:76-87: force, init_timesteps, forward half kick (the half kick
+ * only with NB_ALG_LEAPFROG). */
 int nb_run_begin(nb_handle *h);
+
+/* src/run.jl:171-173: the backward half kick with NB_ALG_LEAPFROG, nothing
+ * with NB_ALG_EULER. */
+int nb_run_end(nb_handle *h);
+
+/* Snapshot schedule: TimeConfig.BetweenSnapshots (src/base/Config.jl:392-394,
+ * 426, 436-439) and TimeInfo.next_output_time_int / _float
+ * (src/base/Config.jl:749-750).  between > 0 sets the first output time to
+ * TimeBegin + between (integer time line: BetweenSnapshotsInt =
+ * floor(between / TimeInterval), which must be >= 1 with adaptive steps);
+ * between = 0 turns output stops off (the default).  Call it before the run,
+ * as the reference fixes the schedule when the Simulation is built; nb_upload
+ * resets the schedule together with the time line.  With a schedule, every
+ * step splits its drift at the output times inside it exactly as
+ * find_next_sync_point_and_drift does (src/base/Timestep.jl:197-215 constant,
+ * :224-245 adaptive): drift to the output time, output, next output time +=
+ * BetweenSnapshots, then drift on to the step's end.  The reference's GPU
+ * drift of constant steps always moves by the full dt
+ * (src/directsumgpu/timestep.jl:67-74); this follows its CPU path. */
+int nb_set_snapshot_interval(nb_handle *h, double between);
+
+/* Up to max_steps steps of step(sim, DirectSum, GPU) that stop at the first
+ * output time reached: then *at_output = 1, the positions are drifted to the
+ * output time (velocities at the half step, as the reference's output
+ * function sees them), nb_get_time gives the output time, and the caller
+ * writes its snapshot (sim.config.output.func, src/base/Timestep.jl:204-206,
+ * 234-236) before calling again, which finishes the interrupted step.
+ * *steps_done counts completed steps.  Without a snapshot schedule this is
+ * nb_step(h, max_steps).  nb_step itself, with a schedule, splits the drifts
+ * the same way but does not stop. */
+int nb_step_until_output(nb_handle *h, int64_t max_steps, int64_t *steps_done,
+                         int32_t *at_output);
+
+/* The snapshot schedule's state: next output time (integer and float; while
+ * stopped at an output, the one after it), whether the time line is stopped
+ * at an output, and the number of output stops so far.  Any pointer may be
+ * NULL. */
+int nb_get_output_time(nb_handle *h, int64_t *next_int, double *next_float, int32_t *at_output,
+                       int64_t *outputs);
 
 /* System time (TimeInfo.system_time_int / system_time_float). */
 int nb_get_time(nb_handle *h, int64_t *t_int, double *t_float);

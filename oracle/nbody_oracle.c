@@ -15,6 +15,8 @@
  *   - init / adaptive kick / const kick      src/base/Timestep.jl:29-93
  *   - leapfrog half kicks                    src/base/Timestep.jl:105-125
  *   - min end step, drift                    src/base/Timestep.jl:135-195
+ *   - drift split at snapshot times          src/base/Timestep.jl:197-245 (find_next_sync_point_and_drift)
+ *   - snapshot schedule                      src/base/Config.jl:436-439, 749-750
  *   - step = drift -> force -> kick          src/directsum/timestep.jl:43-55
  *   - run loop (force, init, half kick, steps, back half kick)  src/run.jl:76-87, 101-173
  *   - kinetic energy, momentum, angular mom. src/base/Energy.jl:13-101
@@ -256,6 +258,23 @@ typedef struct or_state {
     int32_t mond;    /* 0 Newton, 1 Milgrom (1983) */
     double bg_gm, bg_cx, bg_cy, bg_cz, bg_rg;
     double mond_acc0, mond_nu_index;
+    /* TimeConfig.Begin and the snapshot schedule: BetweenSnapshots,
+     * BetweenSnapshotsInt = floor(BetweenSnapshots / TimeInterval) (adaptive)
+     * (src/base/Config.jl:436-439) and TimeInfo.next_output_time_int/_float,
+     * starting at BetweenSnapshotsInt / Begin + BetweenSnapshots
+     * (src/base/Config.jl:749-750). outputs_on 0: no snapshots. */
+    double time_begin;
+    int32_t outputs_on;
+    int32_t pad2;
+    double between_float;
+    int64_t between_int;
+    double next_out_float;
+    int64_t next_out_int;
+    /* Snapshot sink (what sim.config.output.func sees): record k holds
+     * t_float, t_int, then x, y, z, vx, vy, vz (n each); snap_count counts
+     * every output, records beyond snap_cap are not stored. */
+    double *snap;
+    int64_t snap_cap, snap_count;
 } or_state;
 
 static inline double soft_of(const or_state *s, int64_t i) { return s->soft[s->type[i] - 1]; }
@@ -449,6 +468,7 @@ int or_drift_to_int(or_state *s, int64_t next_int)
 {
     s->last_t_int = s->t_int;
     s->t_int = next_int;
+    s->t_float = s->time_begin + (double)s->t_int * s->time_interval;
     double dt = (double)(s->t_int - s->last_t_int) * s->time_interval;
     drift_by(s, dt);
     return OR_OK;
@@ -464,17 +484,55 @@ int or_drift_to_float(or_state *s, double next_float)
     return OR_OK;
 }
 
-/* One step, src/directsum/timestep.jl:43-55 with find_next_sync_point_and_drift
- * (src/base/Timestep.jl:197-245) for the no-snapshot-inside-the-step case. */
+/* sim.config.output.func: one snapshot record of the current state. */
+static void or_output(or_state *s)
+{
+    const int64_t n = s->n;
+    if (s->snap && s->snap_count < s->snap_cap) {
+        double *r = s->snap + s->snap_count * (2 + 6 * n);
+        r[0] = s->t_float;
+        r[1] = (double)s->t_int;
+        memcpy(r + 2 + 0 * n, s->x, sizeof(double) * (size_t)n);
+        memcpy(r + 2 + 1 * n, s->y, sizeof(double) * (size_t)n);
+        memcpy(r + 2 + 2 * n, s->z, sizeof(double) * (size_t)n);
+        memcpy(r + 2 + 3 * n, s->vx, sizeof(double) * (size_t)n);
+        memcpy(r + 2 + 4 * n, s->vy, sizeof(double) * (size_t)n);
+        memcpy(r + 2 + 5 * n, s->vz, sizeof(double) * (size_t)n);
+    }
+    s->snap_count += 1;
+}
+
+/* find_next_sync_point_and_drift: src/base/Timestep.jl:197-215 (constant:
+ * drift to every output time up to t + dt, writing a snapshot at each, then
+ * to t + dt) and :224-245 (adaptive: the same on the integer time line up to
+ * min_endstep). */
+int or_sync_and_drift(or_state *s)
+{
+    if (s->adaptive) {
+        const int64_t mn = or_find_min_endstep(s);
+        if (s->outputs_on && s->between_int <= 0) return OR_ERR_ARG;
+        while (s->outputs_on && s->next_out_int <= mn) {
+            or_drift_to_int(s, s->next_out_int);
+            or_output(s);
+            s->next_out_int += s->between_int;
+        }
+        return or_drift_to_int(s, mn);
+    }
+    const double next_system_time = s->t_float + s->dt;
+    if (s->outputs_on && !(s->between_float > 0.0)) return OR_ERR_ARG;
+    while (s->outputs_on && s->next_out_float <= next_system_time) {
+        or_drift_to_float(s, s->next_out_float);
+        or_output(s);
+        s->next_out_float += s->between_float;
+    }
+    return or_drift_to_float(s, next_system_time);
+}
+
+/* One step, src/directsum/timestep.jl:43-55: find_next_sync_point_and_drift,
+ * force on the active particles, kick. */
 int or_step(or_state *s)
 {
-    int rc;
-    if (s->adaptive) {
-        int64_t mn = or_find_min_endstep(s);
-        rc = or_drift_to_int(s, mn);
-    } else {
-        rc = or_drift_to_float(s, s->t_float + s->dt);
-    }
+    int rc = or_sync_and_drift(s);
     if (rc) return rc;
     rc = or_compute_force(s, 0);
     if (rc) return rc;

@@ -61,6 +61,16 @@ class _State(ctypes.Structure):
         ("bg_rg", ctypes.c_double),
         ("mond_acc0", ctypes.c_double),
         ("mond_nu_index", ctypes.c_double),
+        ("time_begin", ctypes.c_double),
+        ("outputs_on", ctypes.c_int32),
+        ("pad2", ctypes.c_int32),
+        ("between_float", ctypes.c_double),
+        ("between_int", ctypes.c_int64),
+        ("next_out_float", ctypes.c_double),
+        ("next_out_int", ctypes.c_int64),
+        ("snap", _dp),
+        ("snap_cap", ctypes.c_int64),
+        ("snap_count", ctypes.c_int64),
     ]
 
 
@@ -80,7 +90,7 @@ def lib():
             getattr(L, name).argtypes = [ctypes.POINTER(_State), ctypes.c_int]
             getattr(L, name).restype = ctypes.c_int
         for name in ("or_compute_potential", "or_init_timesteps", "or_kick", "or_step",
-                     "or_run_begin", "or_run_end"):
+                     "or_run_begin", "or_run_end", "or_sync_and_drift"):
             getattr(L, name).argtypes = [ctypes.POINTER(_State)]
             getattr(L, name).restype = ctypes.c_int
         L.or_half_kick.argtypes = [ctypes.POINTER(_State), ctypes.c_int]
@@ -166,7 +176,7 @@ class OracleSim:
                  dt=None, eta=0.025, min_step=1e-8, max_step=float("inf"), time_base=1 << 30,
                  time_begin=0.0, time_end=0.1, criterion=CRIT_REF, mode=0, nthreads=0,
                  bg_kind=0, bg_gm=0.0, bg_center=(0.0, 0.0, 0.0), bg_rg=0.0, mond=0,
-                 mond_acc0=0.0, mond_nu_index=2.0):
+                 mond_acc0=0.0, mond_nu_index=2.0, between_snapshots=0.0, max_snapshots=0):
         pos = _f64(pos).reshape(-1, 3)
         vel = _f64(vel).reshape(-1, 3)
         n = pos.shape[0]
@@ -211,6 +221,17 @@ class OracleSim:
         s.mond = mond
         s.mond_acc0 = mond_acc0
         s.mond_nu_index = mond_nu_index
+        # snapshot schedule (src/base/Config.jl:436-439, 749-750)
+        s.time_begin = time_begin
+        s.outputs_on = 1 if between_snapshots > 0 else 0
+        s.between_float = between_snapshots
+        s.between_int = int(np.floor(between_snapshots / s.time_interval)) if s.adaptive else 0
+        s.next_out_float = time_begin + between_snapshots
+        s.next_out_int = s.between_int
+        self._snap = np.zeros((max(max_snapshots, 1), 2 + 6 * n))
+        s.snap = _ptr(self._snap)
+        s.snap_cap = max_snapshots
+        s.snap_count = 0
         self._s = s
 
     def _call(self, name, *args):
@@ -261,6 +282,27 @@ class OracleSim:
 
     def drift_to_float(self, t):
         self._call("or_drift_to_float", t)
+
+    def sync_and_drift(self):
+        """find_next_sync_point_and_drift (src/base/Timestep.jl:197-245)."""
+        self._call("or_sync_and_drift")
+
+    @property
+    def snapshots(self):
+        """Recorded snapshots: list of dicts with t_float, t_int, pos (n,3), vel (n,3)."""
+        out = []
+        n = self.n
+        for k in range(min(self._s.snap_count, self._s.snap_cap)):
+            r = self._snap[k]
+            out.append({"t_float": float(r[0]), "t_int": int(r[1]),
+                        "pos": np.stack([r[2:2 + n], r[2 + n:2 + 2 * n], r[2 + 2 * n:2 + 3 * n]], 1),
+                        "vel": np.stack([r[2 + 3 * n:2 + 4 * n], r[2 + 4 * n:2 + 5 * n],
+                                         r[2 + 5 * n:2 + 6 * n]], 1)})
+        return out
+
+    @property
+    def next_output(self):
+        return self._s.next_out_int, self._s.next_out_float
 
     def step(self, nsteps=1):
         for _ in range(nsteps):
