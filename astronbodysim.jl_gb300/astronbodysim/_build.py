@@ -56,6 +56,8 @@ def build_library(force=False, verbose=False, ptxas_v=False):
             flags = list(COMMON) + ARCH
             if f in FP64_STRICT:
                 flags += ["-fmad=false"]
+            # extra -D tuning definitions (launch-shape experiments)
+            flags += os.environ.get("NBODY_GB300_NVCC_DEFS", "").split()
             if ptxas_v:
                 flags += ["-Xptxas", "-v"]
             jobs.append([nvcc] + flags + ["-c", src, "-o", obj])

@@ -165,6 +165,7 @@ SIGNATURES = {
     "nb_batch_suspend": (ctypes.c_int, [_h, ctypes.c_int64]),
     "nb_batch_resume": (ctypes.c_int, [_h, ctypes.c_int64]),
     "nb_selftest_wait_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_int64, _dp]),
+    "nb_selftest_fp32_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, _dp, _dp]),
     "nb_checkpoint_size": (ctypes.c_int, [_h, _i64p]),
     "nb_checkpoint_save": (ctypes.c_int, [_h, _vp, ctypes.c_int64]),
     "nb_checkpoint_load": (ctypes.c_int, [_h, _vp, ctypes.c_int64]),

@@ -29,6 +29,8 @@ CANDIDATES = [
     {"block": 128, "i_per_thread": 1, "j_split": 2},
     {"block": 128, "i_per_thread": 1, "j_split": 4},
     {"block": 128, "i_per_thread": 2, "j_split": 2},
+    {"block": 128, "i_per_thread": 2, "j_split": 4},
+    {"block": 256, "i_per_thread": 1, "j_split": 2},
     {"block": -1, "i_per_thread": 0, "j_split": 1},  # persistent work list
 ]
 

@@ -35,7 +35,7 @@ struct nb_handle {
     uint32_t* act_scratch = nullptr;
     void* sort_scratch = nullptr;
     float4* pack = nullptr;
-    nb::dvec4* origin = nullptr;
+    nb::TileOrigin* origin = nullptr;
     float4* ext = nullptr;
     int32_t ntiles = 0;
     double* diag_scratch = nullptr;
@@ -67,9 +67,12 @@ struct nb_handle {
 namespace {
 
 constexpr int kTileJ = 256;
-// j-split of the built-in launch rule (the autotuner's choice on GB300 for
-// every N from 2^12 to 2^20, both laws).
+// Built-in launch rule (the autotuner's choice on GB300, both laws): the
+// direct grid of 128-thread CTAs with each i-block's tiles split over 4 CTAs,
+// one target per thread below 2^16 particles and two from 2^16 on (N = 2^20:
+// 351 ms against 367 ms per force).
 constexpr int kAutoJsplit = 4;
+constexpr int64_t kAutoIpt2From = 1 << 16;
 
 int fail(nb_handle* h, int code, const char* fmt, ...) {
     if (h) {
@@ -235,17 +238,17 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
     // Built-in choice (the autotuner's result on GB300, Plummer, both laws,
-    // N = 2^12 .. 2^20): the direct grid with one target per thread and each
-    // i-block's tiles split over 4 CTAs, whose compensated partials are joined
-    // in order.  The split keeps the grid several waves deep at small N, where
-    // the work list was used before.
+    // N = 2^12 .. 2^20): the direct grid with each i-block's tiles split over
+    // 4 CTAs, whose compensated partials are joined in order, and two targets
+    // per thread from 2^16 particles on.  The split keeps the grid several
+    // waves deep at small N, where the work list was used before.
     bool use_wl = h->worklist;
     int blk = h->block, ipt = h->ipt;
     int js = h->jsplit;
     if (h->auto_cfg) {
         use_wl = false;
         blk = 128;
-        ipt = 1;
+        ipt = h->n >= kAutoIpt2From ? 2 : 1;
         js = kAutoJsplit;
     }
     if (particles && use_wl) {
@@ -455,7 +458,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     size_t o_acts = take(sizeof(uint32_t) * (size_t)nb::active_scratch_words(n));
     size_t o_sort = take(nb::sort_scratch_bytes(n));
     size_t o_pack = take(sizeof(float4) * (size_t)npad);
-    size_t o_orig = take(sizeof(nb::dvec4) * (size_t)ntiles);
+    size_t o_orig = take(sizeof(nb::TileOrigin) * (size_t)ntiles);
     size_t o_ext = take(sizeof(float4) * (size_t)ntiles);
     size_t o_ds = take(sizeof(double) * (size_t)dblocks);
     size_t o_do = take(sizeof(double) * 8);
@@ -486,7 +489,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->act_scratch = (uint32_t*)(b + o_acts);
     h->sort_scratch = (void*)(b + o_sort);
     h->pack = (float4*)(b + o_pack);
-    h->origin = (nb::dvec4*)(b + o_orig);
+    h->origin = (nb::TileOrigin*)(b + o_orig);
     h->ext = (float4*)(b + o_ext);
     h->diag_scratch = (double*)(b + o_ds);
     h->diag_blocks = dblocks / 8;

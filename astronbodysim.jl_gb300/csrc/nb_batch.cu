@@ -240,7 +240,8 @@ __global__ void __launch_bounds__(kTileJ)
                  const double* __restrict__ bbox, const int32_t* __restrict__ perm,
                  const double* __restrict__ x, const double* __restrict__ y,
                  const double* __restrict__ z, const double* __restrict__ m,
-                 float4* __restrict__ pack, dvec4* __restrict__ origin, float4* __restrict__ ext) {
+                 float4* __restrict__ pack, TileOrigin* __restrict__ origin,
+                 float4* __restrict__ ext) {
     // The tile's bounding box is reduced in FP32 relative to the tile's first
     // particle c (FP64); the tile origin is c + float offset, and the sources
     // are re-expressed relative to it from their FP64 offsets to c.  The
@@ -305,11 +306,15 @@ __global__ void __launch_bounds__(kTileJ)
     }
     const float oxf = 0.5f * (lo[0] + hi[0]), oyf = 0.5f * (lo[1] + hi[1]), ozf = 0.5f * (lo[2] + hi[2]);
     const double oxd = (double)oxf, oyd = (double)oyf, ozd = (double)ozf;
+    TileOrigin to = make_tile_origin(cx + oxd, cy + oyd, cz + ozd, 0.0);
+    // Sources relative to the origin by the same FP32 steps the force kernel
+    // applies to targets (rel_df): a particle's own entry and its target
+    // coordinates are bit-identical, so the self pair has r = 0.
     float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
     if (valid) {
-        qx = (float)(dx - oxd);
-        qy = (float)(dy - oyd);
-        qz = (float)(dz - ozd);
+        qx = rel_df(split_df(px), to.hi.x, to.lo.x);
+        qy = rel_df(split_df(py), to.hi.y, to.lo.y);
+        qz = rel_df(split_df(pz), to.hi.z, to.lo.z);
         qm = (float)pm;
     }
     float* base = reinterpret_cast<float*>(pack + (int64_t)g * kTileJ);
@@ -326,7 +331,8 @@ __global__ void __launch_bounds__(kTileJ)
         const float amax = fmaxf(fmaxf(fabsf(lo[0]), fabsf(hi[0])),
                                  fmaxf(fmaxf(fabsf(lo[1]), fabsf(hi[1])),
                                        fmaxf(fabsf(lo[2]), fabsf(hi[2]))));
-        origin[g] = make_dvec4(cx + oxd, cy + oyd, cz + ozd, (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
+        to.hi.w = (float)((double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
+        origin[g] = to;
         // box half extents for the near test, enlarged the same way
         const float slack = 4.0e-7f * amax;
         // ext.w: the common source mass when all are equal, else 0 (the pair
@@ -359,7 +365,7 @@ __global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) 
     __shared__ uint32_t done[kStages];
     __shared__ int32_t item_sh;
     __shared__ uint32_t abort_sh;
-    __shared__ double tpx[kFBt], tpy[kFBt], tpz[kFBt];
+    __shared__ float2 tpx[kFBt], tpy[kFBt], tpz[kFBt];
     const int tid = threadIdx.x, lane = tid & 31;
 
     if (tid == 0) {
@@ -406,9 +412,9 @@ __global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) 
                 y = f.y[p];
                 z = f.z[p];
             }
-            tpx[k * BLOCK + tid] = x;
-            tpy[k * BLOCK + tid] = y;
-            tpz[k * BLOCK + tid] = z;
+            tpx[k * BLOCK + tid] = split_df(x);
+            tpy[k * BLOCK + tid] = split_df(y);
+            tpz[k * BLOCK + tid] = split_df(z);
             hh[k] = (float)d.soft[0];
             h2[k] = hh[k] * hh[k];
         }
@@ -424,13 +430,13 @@ __global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) 
             const uint32_t v = vbase + t;
             const int st = (int)(v % kStages);
             const uint32_t par = (v / kStages) & 1u;
-            const dvec4 o = f.origin[d.tile_off + t];
+            const float4 oh = f.origin[d.tile_off + t].hi, ol = f.origin[d.tile_off + t].lo;
             float xr[IPT], yr[IPT], zr[IPT];
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
-                xr[k] = (float)(tpx[k * BLOCK + tid] - o.x);
-                yr[k] = (float)(tpy[k * BLOCK + tid] - o.y);
-                zr[k] = (float)(tpz[k * BLOCK + tid] - o.z);
+                xr[k] = rel_df(tpx[k * BLOCK + tid], oh.x, ol.x);
+                yr[k] = rel_df(tpy[k * BLOCK + tid], oh.y, ol.y);
+                zr[k] = rel_df(tpz[k * BLOCK + tid], oh.z, ol.z);
             }
             float ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll
@@ -651,7 +657,7 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
                               const double* bbox, const int32_t* perm, const double* x,
                               const double* y, const double* z, const double* m, float4* pack,
-                              dvec4* origin, float4* ext, cudaStream_t s) {
+                              TileOrigin* origin, float4* ext, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
     k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, bbox, perm, x, y, z, m, pack, origin, ext);
     return cudaGetLastError();

@@ -71,7 +71,7 @@ struct nb_engine {
     int64_t* steps_slot = nullptr;
     void* sort_scratch = nullptr;
     float4* pack = nullptr;
-    nb::dvec4* origin = nullptr;
+    nb::TileOrigin* origin = nullptr;
     float4* ext = nullptr;
     int32_t* tile_rank = nullptr;
     nb::SysDesc* sysdesc = nullptr;
@@ -477,7 +477,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     size_t o_lperm = take(sizeof(int32_t) * P), o_steps = take(sizeof(int64_t) * S);
     size_t o_sort = take(nb::sort_scratch_bytes(P));
     size_t o_pack = take(sizeof(float4) * kTile * (size_t)e->tile_cap);
-    size_t o_orig = take(sizeof(nb::dvec4) * (size_t)e->tile_cap);
+    size_t o_orig = take(sizeof(nb::TileOrigin) * (size_t)e->tile_cap);
     size_t o_ext = take(sizeof(float4) * (size_t)e->tile_cap);
     size_t o_trank = take(sizeof(int32_t) * (size_t)e->tile_cap);
     size_t o_sd = take(sizeof(nb::SysDesc) * S), o_bs = take(sizeof(nb::BatchSys) * S);
@@ -502,7 +502,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     e->steps_slot = (int64_t*)(b + o_steps);
     e->sort_scratch = b + o_sort;
     e->pack = (float4*)(b + o_pack);
-    e->origin = (nb::dvec4*)(b + o_orig);
+    e->origin = (nb::TileOrigin*)(b + o_orig);
     e->ext = (float4*)(b + o_ext);
     e->tile_rank = (int32_t*)(b + o_trank);
     e->sysdesc = (nb::SysDesc*)(b + o_sd);

@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
                                                  const double* __restrict__ m, int64_t n,
                                                  const int32_t* __restrict__ perm,
                                                  float4* __restrict__ pack,
-                                                 dvec4* __restrict__ origin,
+                                                 TileOrigin* __restrict__ origin,
                                                  float4* __restrict__ ext) {
     __shared__ double red[8][kTileJ / 32];
     const int64_t i = (int64_t)blockIdx.x * kTileJ + threadIdx.x;
@@ -95,13 +95,22 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
     const double ox = 0.5 * (lo[0] + hi[0]);
     const double oy = 0.5 * (lo[1] + hi[1]);
     const double oz = 0.5 * (lo[2] + hi[2]);
+    const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+    const TileOrigin to = make_tile_origin(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
+    // Sources relative to the origin by the same FP32 steps the force kernels
+    // apply to targets (rel_df), so a particle's own source entry and its
+    // target coordinates are bit-identical and the self pair has r = 0.
     float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
     if (valid) {
-        qx = (float)(px - ox);
-        qy = (float)(py - oy);
-        qz = (float)(pz - oz);
+        qx = rel_df(split_df(px), to.hi.x, to.lo.x);
+        qy = rel_df(split_df(py), to.hi.y, to.lo.y);
+        qz = rel_df(split_df(pz), to.hi.z, to.lo.z);
         qm = (float)pm;
     }
+    // A full tile of one common mass keeps that mass in ext.w only; its mass
+    // slots hold |q|^2 for the expanded far loop (pair_loop_expand).  Every
+    // pair loop takes the mass of such a tile from ext.w.
+    if (mu > 0.0f) qm = fmaf(qx, qx, fmaf(qy, qy, qz * qz));
     // (Zero-mass padding far away contributes exactly 0 and never takes the
     // r < h path.)  Paired layout: sources 2p and 2p+1 of the tile occupy
     // float4 (x0, x1, y0, y1) and float4 (z0, z1, m0, m1).
@@ -112,8 +121,7 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
     base[8 * pr + 4 + half] = qz;
     base[8 * pr + 6 + half] = qm;
     if (threadIdx.x == 0) {
-        const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
-        origin[blockIdx.x] = make_dvec4(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
+        origin[blockIdx.x] = to;
         // Half extents of the box for the near test, rounded up and enlarged to
         // cover the rounding of the FP32 relative coordinates (the test must
         // never under-estimate them).
@@ -127,8 +135,8 @@ __global__ void __launch_bounds__(kTileJ) k_pack(const double* __restrict__ x,
 }
 
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
-                        int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
-                        float4* ext, cudaStream_t s) {
+                        int64_t n, const int32_t* perm, int tile_j, float4* pack,
+                        TileOrigin* origin, float4* ext, cudaStream_t s) {
     if (tile_j != kTileJ) return cudaErrorInvalidValue;
     if (n <= 0) return cudaSuccess;
     const int64_t ntiles = (n + kTileJ - 1) / kTileJ;
@@ -140,8 +148,10 @@ cudaError_t launch_pack(const double* x, const double* y, const double* z, const
 // Force kernel.
 //
 // CTA = BLOCK threads, IPT targets per thread (slot k*BLOCK + tid).  Targets'
-// FP64 positions live in shared memory; per j-tile each thread re-expresses
-// them relative to the tile origin in FP64 and rounds to FP32.
+// FP64 positions live in shared memory as float pairs hi + lo; per j-tile each
+// thread re-expresses them relative to the tile origin (also hi + lo) with
+// three FP32 operations per coordinate, so the tile loop issues no FP64
+// instruction.
 //
 // j-tiles stream through a kStages ring.  full[s] (mbarrier, count 1 +
 // transaction bytes) completes when the bulk copy of the tile has landed.
@@ -151,15 +161,32 @@ cudaError_t launch_pack(const double* x, const double* y, const double* z, const
 // tiles apart.  Every wait is bounded; a timed-out warp records
 // DEVERR_TIMEOUT and stops, and the CTA drains its copies before exiting.
 // ---------------------------------------------------------------------------
+// CTAs per SM the register allocation is held to (acceleration-only launches
+// of 128 threads); overridable at build time for launch-shape experiments.
+#ifndef NB_MINB_IPT1
+#define NB_MINB_IPT1 6
+#endif
+#ifndef NB_MINB_IPT2
+#define NB_MINB_IPT2 5
+#endif
+#ifndef NB_MINB_IPT4
+#define NB_MINB_IPT4 1
+#endif
+template <int BLOCK, int IPT, bool POT>
+struct ForceOcc {
+    static constexpr int value =
+        (BLOCK == 128 && !POT) ? (IPT == 1 ? NB_MINB_IPT1 : (IPT == 2 ? NB_MINB_IPT2 : NB_MINB_IPT4)) : 1;
+};
+
 template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && !POT) ? (IPT == 2 ? 8 : (IPT == 1 ? 6 : 1)) : 1) k_force_mixed(Sources32 src, Targets tg, double G,
+__global__ void __launch_bounds__(BLOCK, (ForceOcc<BLOCK, IPT, POT>::value)) k_force_mixed(Sources32 src, Targets tg, double G,
                                                        uint32_t* __restrict__ err) {
     constexpr int kWarpsPerCta = BLOCK / 32;
     __shared__ __align__(128) float4 buf[kStages * kTileJ];
     __shared__ __align__(8) uint64_t full[kStages];
     __shared__ uint32_t done[kStages];
     __shared__ uint32_t abort_flag;
-    __shared__ double tpx[BLOCK * IPT], tpy[BLOCK * IPT], tpz[BLOCK * IPT];
+    __shared__ float2 tpx[BLOCK * IPT], tpy[BLOCK * IPT], tpz[BLOCK * IPT];
 
     const int64_t ntg = tg.d_count ? (int64_t)(*tg.d_count) : tg.n;
     const int js = src.jsplit > 1 ? src.jsplit : 1;
@@ -197,9 +224,9 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && !POT) ? (IPT == 2 ? 8 
             z = tg.z[p];
             if (tg.type) h = tg.soft[tg.type[p] - 1];
         }
-        tpx[k * BLOCK + tid] = x;
-        tpy[k * BLOCK + tid] = y;
-        tpz[k * BLOCK + tid] = z;
+        tpx[k * BLOCK + tid] = split_df(x);
+        tpy[k * BLOCK + tid] = split_df(y);
+        tpz[k * BLOCK + tid] = split_df(z);
         hh[k] = (float)h;
         h2[k] = hh[k] * hh[k];
     }
@@ -224,13 +251,13 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && !POT) ? (IPT == 2 ? 8 
     for (int t = 0; t < ntiles; ++t) {
         const int s = t % kStages;
         const uint32_t par = (uint32_t)(t / kStages) & 1u;
-        const dvec4 o = src.origin[t_lo + t];
+        const float4 oh = src.origin[t_lo + t].hi, ol = src.origin[t_lo + t].lo;
         float xr[IPT], yr[IPT], zr[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
-            xr[k] = (float)(tpx[k * BLOCK + tid] - o.x);
-            yr[k] = (float)(tpy[k * BLOCK + tid] - o.y);
-            zr[k] = (float)(tpz[k * BLOCK + tid] - o.z);
+            xr[k] = rel_df(tpx[k * BLOCK + tid], oh.x, ol.x);
+            yr[k] = rel_df(tpy[k * BLOCK + tid], oh.y, ol.y);
+            zr[k] = rel_df(tpz[k * BLOCK + tid], oh.z, ol.z);
         }
         float ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll
@@ -249,12 +276,15 @@ __global__ void __launch_bounds__(BLOCK, (BLOCK == 128 && !POT) ? (IPT == 2 ? 8 
         // Warp-uniform choice of the pair loop: when every target of the warp
         // lies farther than (tile radius + h) from the tile origin, no pair of
         // this tile can have r < h and the branch-free loop runs.
+        const float4 ex = src.ext[t_lo + t];
         bool near = false;
-        if (LAW == NB_LAW_SPLINE_G2) near = warp_near<IPT>(src.ext[t_lo + t], xr, yr, zr, hh, pidx);
+        if (LAW == NB_LAW_SPLINE_G2) near = warp_near<IPT>(ex, xr, yr, zr, hh, pidx);
         if (near)
-            pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, src.ext[t_lo + t].w);
+            pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, ex.w);
+        else if (ex.w > 0.0f && warp_expandable<IPT>(oh.w, xr, yr, zr, pidx))
+            pair_loop_expand<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);
         else
-            pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, src.ext[t_lo + t].w);
+            pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);
 
         // Release stage s; the last warp out refills it with tile t + kStages.
         __syncwarp();

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kWBlock, (ACC && !POT) ? 8 : 1) k_force_workli
     __shared__ __align__(8) uint64_t full[kStages];
     __shared__ uint32_t done[kStages];
     __shared__ uint32_t issued;
-    __shared__ double tpx[kWBt], tpy[kWBt], tpz[kWBt];
+    __shared__ float2 tpx[kWBt], tpy[kWBt], tpz[kWBt];
 
     int32_t nb0, ntg0;
     const int64_t U = total_units(w, nb0, ntg0);
@@ -184,9 +184,9 @@ __global__ void __launch_bounds__(kWBlock, (ACC && !POT) ? 8 : 1) k_force_workli
                     z = w.z[p];
                     if (w.type) h = d.soft[w.type[p] - 1];
                 }
-                tpx[k * BLOCK + tid] = x;
-                tpy[k * BLOCK + tid] = y;
-                tpz[k * BLOCK + tid] = z;
+                tpx[k * BLOCK + tid] = split_df(x);
+                tpy[k * BLOCK + tid] = split_df(y);
+                tpz[k * BLOCK + tid] = split_df(z);
                 hh[k] = (float)h;
                 h2[k] = hh[k] * hh[k];
                 sx[k] = sy[k] = sz[k] = sp[k] = 0.0f;
@@ -195,13 +195,13 @@ __global__ void __launch_bounds__(kWBlock, (ACC && !POT) ? 8 : 1) k_force_workli
         }
         const int st = (int)(v % kStages);
         const uint32_t par = (uint32_t)(v / kStages) & 1u;
-        const dvec4 o = w.origin[cur.tile_off + cur.t];
+        const float4 oh = w.origin[cur.tile_off + cur.t].hi, ol = w.origin[cur.tile_off + cur.t].lo;
         float xr[IPT], yr[IPT], zr[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; ++k) {
-            xr[k] = (float)(tpx[k * BLOCK + tid] - o.x);
-            yr[k] = (float)(tpy[k * BLOCK + tid] - o.y);
-            zr[k] = (float)(tpz[k * BLOCK + tid] - o.z);
+            xr[k] = rel_df(tpx[k * BLOCK + tid], oh.x, ol.x);
+            yr[k] = rel_df(tpy[k * BLOCK + tid], oh.y, ol.y);
+            zr[k] = rel_df(tpz[k * BLOCK + tid], oh.z, ol.z);
         }
         float ax[IPT], ay[IPT], az[IPT], ap[IPT];
 #pragma unroll

@@ -17,6 +17,31 @@ __host__ __device__ __forceinline__ dvec4 make_dvec4(double x, double y, double 
     return dvec4{x, y, z, w};
 }
 
+// FP64 tile origin (or target position) held as an unevaluated sum of two
+// floats, v = hi + lo with lo = fl(v - hi).  x - o then costs three FP32
+// operations, (x.hi - o.hi) + (x.lo - o.lo), within about one FP32 ulp of the
+// FP64 difference rounded once, so the force kernels' per-tile re-origin
+// needs no FP64 instruction.  hi.w carries the tile's half diagonal.
+struct __align__(16) TileOrigin {
+    float4 hi;
+    float4 lo;
+};
+__device__ __forceinline__ float2 split_df(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+__device__ __forceinline__ TileOrigin make_tile_origin(double x, double y, double z, double w) {
+    const float2 a = split_df(x), b = split_df(y), c = split_df(z);
+    TileOrigin o;
+    o.hi = make_float4(a.x, b.x, c.x, (float)w);
+    o.lo = make_float4(a.y, b.y, c.y, 0.0f);
+    return o;
+}
+// FP32 coordinate of a split position t relative to a split origin (oh, ol).
+__device__ __forceinline__ float rel_df(float2 t, float oh, float ol) {
+    return __fadd_rn(__fsub_rn(t.x, oh), __fsub_rn(t.y, ol));
+}
+
 // Device error word bits (read back by the host after synchronising calls).
 enum : uint32_t {
     DEVERR_NONFINITE = 1u,  // NaN/Inf acceleration
@@ -99,7 +124,7 @@ struct Targets {
 // float4 (x - o, y - o, z - o, m) with an FP64 origin o per tile.
 struct Sources32 {
     const float4* pack;
-    const dvec4* origin;
+    const TileOrigin* origin;
     const float4* ext;  // per tile: half extents of the box (x, y, z) and half diagonal
     int32_t ntiles;
     int32_t tile_j;
@@ -142,7 +167,7 @@ struct WorkList {
     const int32_t* d_count;
     const int32_t* perm;       // otherwise target slot q of system s is particle perm[off + q]
     const float4* pack;
-    const dvec4* origin;
+    const TileOrigin* origin;
     const float4* ext;
     const double* x;
     const double* y;
@@ -183,7 +208,7 @@ struct BatchForce {
     int32_t* counter;     // claim counter, zeroed by the launch
     const int32_t* perm;  // sorted slot -> arena particle
     const float4* pack;
-    const dvec4* origin;
+    const TileOrigin* origin;
     const float4* ext;
     const double* x;
     const double* y;
@@ -211,7 +236,7 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
                               const double* bbox, const int32_t* perm, const double* x,
                               const double* y, const double* z, const double* m, float4* pack,
-                              dvec4* origin, float4* ext, cudaStream_t s);
+                              TileOrigin* origin, float4* ext, cudaStream_t s);
 int batch_small_sort_limit();
 cudaError_t prepare_batch_sort_small();
 cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t max_small_n,
@@ -231,8 +256,8 @@ cudaError_t launch_batch_kick(double* vx, double* vy, double* vz, const double* 
 
 // Launch helpers implemented in the .cu files.
 cudaError_t launch_pack(const double* x, const double* y, const double* z, const double* m,
-                        int64_t n, const int32_t* perm, int tile_j, float4* pack, dvec4* origin,
-                        float4* ext, cudaStream_t s);
+                        int64_t n, const int32_t* perm, int tile_j, float4* pack,
+                        TileOrigin* origin, float4* ext, cudaStream_t s);
 // Morton-order permutation of the particles (nb_sort.cu); scratch of
 // sort_scratch_bytes(n) bytes.
 size_t sort_scratch_bytes(int64_t n);
@@ -372,6 +397,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 __device__ __forceinline__ float rsqrt_approx(float x) {
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Approximate reciprocal (MUFU), flushing subnormals; used for r^-2 so that
+// m r^-3 = (m r^-1) * r^-2 costs one FP32 multiply after the two MUFU ops.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
 }
 

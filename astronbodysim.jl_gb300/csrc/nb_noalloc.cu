@@ -38,7 +38,7 @@ constexpr size_t al256(size_t v) { return (v + 255) / 256 * 256; }
 constexpr size_t kOffPerm = 0;
 constexpr size_t kOffPack = kOffPerm + al256(sizeof(int32_t) * kNoAllocMaxParticles);
 constexpr size_t kOffOrigin = kOffPack + al256(sizeof(float4) * kNoAllocMaxParticles);
-constexpr size_t kOffExt = kOffOrigin + al256(sizeof(nb::dvec4) * (kNoAllocMaxParticles / kTile));
+constexpr size_t kOffExt = kOffOrigin + al256(sizeof(nb::TileOrigin) * (kNoAllocMaxParticles / kTile));
 constexpr size_t kOffErr = kOffExt + al256(sizeof(float4) * (kNoAllocMaxParticles / kTile));
 constexpr size_t kOffSort = kOffErr + 256;
 // Upper bound of the radix-sort scratch for kNoAllocMaxParticles (two key
@@ -119,7 +119,7 @@ extern "C" int nb_force_noalloc(int64_t n, const double* x, const double* y, con
     char* b = static_cast<char*>(base);
     int32_t* perm = reinterpret_cast<int32_t*>(b + kOffPerm);
     float4* pack = reinterpret_cast<float4*>(b + kOffPack);
-    nb::dvec4* origin = reinterpret_cast<nb::dvec4*>(b + kOffOrigin);
+    nb::TileOrigin* origin = reinterpret_cast<nb::TileOrigin*>(b + kOffOrigin);
     float4* ext = reinterpret_cast<float4*>(b + kOffExt);
     uint32_t* err = reinterpret_cast<uint32_t*>(b + kOffErr);
     void* sort_scratch = b + kOffSort;

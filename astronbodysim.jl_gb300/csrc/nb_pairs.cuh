@@ -9,6 +9,25 @@ namespace nb {
 
 constexpr int kTileJ = 256;
 constexpr int kStages = 4;
+
+// Pair-loop shape: sets of split partial sums per target (consecutive source
+// pairs alternate between them, so accumulating FMAs do not wait on each
+// other) and source pairs per unrolled iteration.  Overridable at build time
+// (-DNB_SPLIT_SUMS_IPT1=..., for launch-shape experiments).
+#ifndef NB_SPLIT_SUMS_IPT1
+#define NB_SPLIT_SUMS_IPT1 2
+#endif
+#ifndef NB_SPLIT_SUMS_IPTN
+#define NB_SPLIT_SUMS_IPTN 1
+#endif
+#ifndef NB_PAIRS_PER_ITER
+#define NB_PAIRS_PER_ITER 4
+#endif
+template <int IPT>
+struct LoopShape {
+    static constexpr int NA = IPT == 1 ? NB_SPLIT_SUMS_IPT1 : NB_SPLIT_SUMS_IPTN;
+    static constexpr int UNROLL = NB_PAIRS_PER_ITER / NA > 0 ? NB_PAIRS_PER_ITER / NA : 1;
+};
 constexpr uint64_t kWaitTimeoutNs = 2000000000ull;  // 2 s
 
 // ---------------------------------------------------------------------------
@@ -81,7 +100,7 @@ __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, con
     // With one target per thread the sums are split over two sets (even and
     // odd source pairs) so that consecutive accumulating FMAs do not wait on
     // each other; with more targets per thread they are independent already.
-    constexpr int NA = (IPT == 1) ? 2 : 1;
+    constexpr int NA = LoopShape<IPT>::NA;
     float2 nx[IPT], ny[IPT], nz[IPT], e2[IPT];
     float2 sx[NA][IPT], sy[NA][IPT], sz[NA][IPT], sp[NA][IPT];
 #pragma unroll
@@ -93,7 +112,7 @@ __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, con
 #pragma unroll
         for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
-#pragma unroll (4 / NA)
+#pragma unroll (LoopShape<IPT>::UNROLL)
     for (int p = 0; p < kTileJ / 2; p += NA) {
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
@@ -144,6 +163,100 @@ __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, con
     }
 }
 
+// Far-tile loop in expanded form, for full uniform-mass tiles (the pack then
+// stores |q|^2 in each source's mass slot) seen from targets at least
+// kExpandRatio tile radii from the tile origin:
+//   r^2 = (|q|^2 + |x|^2 [+ h^2]) - 2 q.x            (4 FP32 operations)
+//   sum_j (q_j - x) r_j^-3 = sum_j q_j r_j^-3 - x sum_j r_j^-3
+// so the three differences q - x drop out of the pair loop: 10 FP32
+// operations per interaction instead of 11 (the MUFU rsqrt unchanged).  With
+// |x| >= 2.5 |q|, (|x|^2 + |q|^2) / |x - q|^2 <= 1.16 / 0.36 = 3.2, so the
+// rounding of r^2 (about 3 ulp of |x|^2 + |q|^2) stays within about 10 ulp of
+// r^2, and sum q r^-3 - x sum r^-3 cancels by at most 1.4 / 0.6 = 7/3.
+// (Measured at N = 2^20: median and p99 relative force errors 2.6e-8 and
+// 4.9e-7, as with the difference form alone.)
+#ifndef NB_EXPAND_RATIO
+#define NB_EXPAND_RATIO 2.5f
+#endif
+constexpr float kExpandRatio = NB_EXPAND_RATIO;
+
+template <int IPT>
+__device__ __forceinline__ bool warp_expandable(float radius, const float* xr, const float* yr,
+                                                const float* zr, const int32_t* pidx) {
+    bool ok = true;
+    const float lim = kExpandRatio * radius;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const float x2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
+        ok &= (pidx[k] < 0) || (x2 >= lim * lim);
+    }
+    return __all_sync(0xffffffffu, ok);
+}
+
+template <int LAW, bool ACC, bool POT, int IPT>
+__device__ __forceinline__ void pair_loop_expand(const float4* __restrict__ b, const float* xr,
+                                                 const float* yr, const float* zr,
+                                                 const float* h2, float* ax, float* ay, float* az,
+                                                 float* ap, float mu) {
+    constexpr int NA = LoopShape<IPT>::NA;
+    float2 mx[IPT], my[IPT], mz[IPT], cc[IPT];
+    float2 sx[NA][IPT], sy[NA][IPT], sz[NA][IPT], sw[NA][IPT], sp[NA][IPT];
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        mx[k] = make_float2(-2.0f * xr[k], -2.0f * xr[k]);
+        my[k] = make_float2(-2.0f * yr[k], -2.0f * yr[k]);
+        mz[k] = make_float2(-2.0f * zr[k], -2.0f * zr[k]);
+        float c = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
+        if (LAW == NB_LAW_PLUMMER) c += h2[k];
+        cc[k] = make_float2(c, c);
+#pragma unroll
+        for (int u = 0; u < NA; ++u)
+            sx[u][k] = sy[u][k] = sz[u][k] = sw[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
+    }
+#pragma unroll (LoopShape<IPT>::UNROLL)
+    for (int p = 0; p < kTileJ / 2; p += NA) {
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+            const float4 A = b[2 * (p + u)];
+            const float4 B = b[2 * (p + u) + 1];
+            const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+            const float2 qz = make_float2(B.x, B.y), qq = make_float2(B.z, B.w);
+#pragma unroll
+            for (int k = 0; k < IPT; ++k) {
+                float2 r2 = __fadd2_rn(qq, cc[k]);
+                r2 = __ffma2_rn(qz, mz[k], r2);
+                r2 = __ffma2_rn(qy, my[k], r2);
+                r2 = __ffma2_rn(qx, mx[k], r2);
+                const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
+                if (ACC) {
+                    const float2 r3 = __fmul2_rn(__fmul2_rn(rinv, rinv), rinv);
+                    sx[u][k] = __ffma2_rn(qx, r3, sx[u][k]);
+                    sy[u][k] = __ffma2_rn(qy, r3, sy[u][k]);
+                    sz[u][k] = __ffma2_rn(qz, r3, sz[u][k]);
+                    sw[u][k] = __fadd2_rn(sw[u][k], r3);
+                }
+                if (POT) sp[u][k] = __fadd2_rn(sp[u][k], rinv);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        float tx = 0.0f, ty = 0.0f, tz = 0.0f, tw = 0.0f, tp = 0.0f;
+#pragma unroll
+        for (int u = 0; u < NA; ++u) {
+            tx += sx[u][k].x + sx[u][k].y;
+            ty += sy[u][k].x + sy[u][k].y;
+            tz += sz[u][k].x + sz[u][k].y;
+            tw += sw[u][k].x + sw[u][k].y;
+            tp += sp[u][k].x + sp[u][k].y;
+        }
+        ax[k] += fmaf(-xr[k], tw, tx) * mu;
+        ay[k] += fmaf(-yr[k], tw, ty) * mu;
+        az[k] += fmaf(-zr[k], tw, tz) * mu;
+        ap[k] += tp * mu;
+    }
+}
+
 // Far-tile dispatch: the uniform-mass loop when the pack flagged the tile.
 template <int LAW, bool ACC, bool POT, int IPT>
 __device__ __forceinline__ void pair_loop_far(const float4* __restrict__ b, const float* xr,
@@ -169,7 +282,7 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
     // source pairs held such a half.  Pass 2 revisits only the blocks that
     // some lane of the warp flagged and adds the spline terms of their r < h
     // pairs.
-    constexpr int NA = (IPT == 1) ? 2 : 1;
+    constexpr int NA = LoopShape<IPT>::NA;
     float2 nx[IPT], ny[IPT], nz[IPT];
     float2 sx[NA][IPT], sy[NA][IPT], sz[NA][IPT], sp[NA][IPT];
     uint32_t blk = 0;  // bit q: a r < h half among source pairs 8q .. 8q + 7
@@ -181,7 +294,7 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
 #pragma unroll
         for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
-#pragma unroll (4 / NA)
+#pragma unroll (LoopShape<IPT>::UNROLL)
     for (int p = 0; p < kTileJ / 2; p += NA) {
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
@@ -256,7 +369,7 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
                 if (__any_sync(0xffffffffu, cx | cy)) {
                     if (cx) {
                         float mr3, mp;
-                        spline_close(r2.x, rsqrt_approx(r2.x), qm.x, hh[k], mr3, mp);
+                        spline_close(r2.x, rsqrt_approx(r2.x), UNI ? mu : qm.x, hh[k], mr3, mp);
                         tx[k].x = fmaf(dx.x, mr3, tx[k].x);
                         ty[k].x = fmaf(dy.x, mr3, ty[k].x);
                         tz[k].x = fmaf(dz.x, mr3, tz[k].x);
@@ -264,7 +377,7 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
                     }
                     if (cy) {
                         float mr3, mp;
-                        spline_close(r2.y, rsqrt_approx(r2.y), qm.y, hh[k], mr3, mp);
+                        spline_close(r2.y, rsqrt_approx(r2.y), UNI ? mu : qm.y, hh[k], mr3, mp);
                         tx[k].y = fmaf(dx.y, mr3, tx[k].y);
                         ty[k].y = fmaf(dy.y, mr3, ty[k].y);
                         tz[k].y = fmaf(dz.y, mr3, tz[k].y);

@@ -45,3 +45,94 @@ extern "C" int nb_selftest_wait_timeout(int device, int64_t timeout_ns, double* 
     if (waited_ms) *waited_ms = (double)ns * 1e-6;
     return (bits & nb::DEVERR_TIMEOUT) ? NB_ERR_TIMEOUT : NB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// FP32 throughput probe: the denominator of the force kernel's roofline,
+// measured instead of assumed.  Every thread runs 8 independent dependency
+// chains a = a * b + c (scalar fma.rn.f32, or packed fma.rn.f32x2 on float2),
+// so the FMA pipe, not latency, bounds the rate.  Grid: 4 CTAs of 256 threads
+// per SM.  The chains stay finite (|b| < 1); one thread stores a value that
+// depends on every chain so nothing is dead code.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kPeakThreads = 256;
+constexpr int kPeakChains = 8;
+
+__global__ void __launch_bounds__(kPeakThreads) k_fma_scalar(int iters, float b, float c,
+                                                              float* sink) {
+    float a[kPeakChains];
+#pragma unroll
+    for (int k = 0; k < kPeakChains; ++k) a[k] = (float)(threadIdx.x + k) * 1e-3f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+#pragma unroll
+            for (int k = 0; k < kPeakChains; ++k) a[k] = __fmaf_rn(a[k], b, c);
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kPeakChains; ++k) s += a[k];
+    if (s == 12345.0f) *sink = s;  // never true for these inputs; keeps the chains live
+}
+
+__global__ void __launch_bounds__(kPeakThreads) k_fma_packed(int iters, float b, float c,
+                                                              float* sink) {
+    float2 a[kPeakChains];
+    const float2 b2 = make_float2(b, b), c2 = make_float2(c, c);
+#pragma unroll
+    for (int k = 0; k < kPeakChains; ++k)
+        a[k] = make_float2((float)(threadIdx.x + k) * 1e-3f, (float)(threadIdx.x - k) * 1e-3f);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+#pragma unroll
+            for (int k = 0; k < kPeakChains; ++k) a[k] = __ffma2_rn(a[k], b2, c2);
+        }
+    }
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < kPeakChains; ++k) s += a[k].x + a[k].y;
+    if (s == 12345.0f) *sink = s;
+}
+
+}  // namespace
+
+extern "C" int nb_selftest_fp32_peak(int device, int packed, double* tflops, double* ms) {
+    if (cudaSetDevice(device) != cudaSuccess) return NB_ERR_CUDA;
+    int nsm = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return NB_ERR_CUDA;
+    float* sink = nullptr;
+    if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess) return NB_ERR_OOM;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const int grid = 4 * nsm;
+    const int iters = 4096;  // x 16 x 8 chains per thread
+    const double lanes_per_op = packed ? 2.0 : 1.0;
+    const double flop = 2.0 * lanes_per_op * (double)grid * kPeakThreads * iters * 16.0 * kPeakChains;
+    float best = 1e30f;
+    cudaError_t e = cudaSuccess;
+    for (int rep = 0; rep < 6 && e == cudaSuccess; ++rep) {
+        cudaEventRecord(e0);
+        if (packed)
+            k_fma_packed<<<grid, kPeakThreads>>>(iters, 0.9999f, 1e-4f, sink);
+        else
+            k_fma_scalar<<<grid, kPeakThreads>>>(iters, 0.9999f, 1e-4f, sink);
+        cudaEventRecord(e1);
+        e = cudaEventSynchronize(e1);
+        float t = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+        if (rep > 0 && t < best) best = t;  // first launch is the warm-up
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    if (e != cudaSuccess) return NB_ERR_CUDA;
+    if (ms) *ms = best;
+    if (tflops) *tflops = flop / (best * 1e-3) / 1e12;
+    return NB_OK;
+}

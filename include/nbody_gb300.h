@@ -368,6 +368,14 @@ const char *nb_engine_last_error(nb_engine *e);
  * *waited_ms; the device context stays usable. */
 int nb_selftest_wait_timeout(int device, int64_t timeout_ns, double *waited_ms);
 
+/* FP32 throughput probe (no counterpart in the reference; it measures the
+ * denominator of the force kernel's roofline): 4 CTAs x 256 threads per SM,
+ * each thread running 8 independent chains of fma.rn.f32 (packed = 0) or
+ * fma.rn.f32x2 (packed = 1, two lanes per instruction), timed with CUDA
+ * events (best of 5 after a warm-up launch).  *tflops counts 2 flop per FMA
+ * lane. */
+int nb_selftest_fp32_peak(int device, int packed, double *tflops, double *ms);
+
 /* Last error message of this handle (never NULL). */
 const char *nb_last_error(nb_handle *h);
 
