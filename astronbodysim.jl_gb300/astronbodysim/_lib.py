@@ -74,6 +74,8 @@ class nb_params(ctypes.Structure):
         ("bg_rg", ctypes.c_double),
         ("mond_acc0", ctypes.c_double),
         ("mond_nu_index", ctypes.c_double),
+        ("stages", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

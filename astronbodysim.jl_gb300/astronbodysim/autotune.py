@@ -2,10 +2,12 @@
 
 For each particle count it times nb_compute_force (mixed precision) with
 every candidate shape -- the direct grid with (threads per CTA, targets per
-thread, CTAs sharing an i-block's sources) over {128, 256} x {1, 2, 4} x
-{1, 2, 4}, and the persistent work-list kernel -- using
-CUDA events on the handle's stream, and records the fastest in a JSON table
-(tuning_gb300.json next to this file, or a path given by the caller).
+thread, CTAs sharing an i-block's sources) from {128, 256} x {1, 2, 4} x
+{1, .., 8}, and the persistent work-list kernel -- using CUDA events on the
+handle's stream; then, at the fastest of those, the j-tile size (128, 256,
+512 sources) and the depth of the shared-memory ring (3, 4, 6 stages).  The
+fastest shape goes into a JSON table (tuning_gb300.json next to this file, or
+a path given by the caller) as "block x targets x j-split x tile x stages".
 Simulation(tuning=...) looks the table up by the nearest particle count of the
 same law; without a table the library's built-in rule applies.
 """
@@ -29,6 +31,10 @@ CANDIDATES = [
     {"block": 128, "i_per_thread": 1, "j_split": 2},
     {"block": 128, "i_per_thread": 1, "j_split": 4},
     {"block": 128, "i_per_thread": 2, "j_split": 2},
+    {"block": 128, "i_per_thread": 2, "j_split": 4},
+    {"block": 128, "i_per_thread": 2, "j_split": 8},
+    {"block": 128, "i_per_thread": 1, "j_split": 8},
+    {"block": 256, "i_per_thread": 1, "j_split": 2},
     {"block": 128, "i_per_thread": 2, "j_split": 4},
     {"block": 256, "i_per_thread": 1, "j_split": 2},
     {"block": -1, "i_per_thread": 0, "j_split": 1},  # persistent work list
@@ -55,6 +61,13 @@ def _time_force(sim, reps):
     return float(np.median(times))
 
 
+TILES = [(128, 3), (128, 4), (128, 6), (256, 3), (256, 6), (512, 3), (512, 4)]
+
+
+def shape_key(block, ipt, js, tile=256, stages=4):
+    return "%dx%dx%dx%dx%d" % (block, ipt, js, tile, stages)
+
+
 def tune(sizes, law="spline", reps=3, eps=1e-3, seed=0, log=print):
     """Returns {"law": law, "entries": [{"n", "best", "ms": {shape: ms}}]}."""
     from .sim import Simulation
@@ -63,14 +76,26 @@ def tune(sizes, law="spline", reps=3, eps=1e-3, seed=0, log=print):
     for n in sizes:
         data = plummer(int(n), seed=seed)
         res = {}
-        for c in CANDIDATES:
+
+        def run(block, ipt, js, tile=0, stages=0):
             sim = Simulation(data, ForceSofteningTable=[eps] * 6, TimeStep=1e-4, precision="mixed",
-                             law=law, block=c["block"], i_per_thread=c["i_per_thread"],
-                             j_split=c["j_split"])
-            key = "worklist" if c["block"] == -1 else "%dx%dx%d" % (c["block"], c["i_per_thread"],
-                                                                    c["j_split"])
-            res[key] = _time_force(sim, reps)
+                             law=law, block=block, i_per_thread=ipt, j_split=js, tile_j=tile,
+                             stages=stages)
+            ms = _time_force(sim, reps)
             sim.close()
+            return ms
+
+        for c in CANDIDATES:
+            if c["block"] == -1:
+                res["worklist"] = run(-1, 0, 1)
+            else:
+                res[shape_key(c["block"], c["i_per_thread"], c["j_split"])] = run(
+                    c["block"], c["i_per_thread"], c["j_split"])
+        grid = min((k for k in res if k != "worklist"), key=res.get)
+        b, i, j = (int(v) for v in grid.split("x")[:3])
+        if b == 128 and i in (1, 2):
+            for t, s in TILES:
+                res[shape_key(b, i, j, t, s)] = run(b, i, j, t, s)
         best = min(res, key=res.get)
         entries.append({"n": int(n), "best": best, "ms": res,
                         "g_interactions_per_s": float(n) * n / (res[best] / 1e3) / 1e9})
@@ -140,14 +165,16 @@ def load(path=DEFAULT_TABLE):
 
 
 def lookup(n, law="spline", path=DEFAULT_TABLE):
-    """(block, i_per_thread, j_split) of the tuned shape nearest to n in log
-    space, or None."""
+    """(block, i_per_thread, j_split, tile_j, stages) of the tuned shape
+    nearest to n in log space, or None."""
     t = load(path)
     if not t or law not in t or not t[law] or not isinstance(t[law], list):
         return None
     e = min(t[law], key=lambda e: abs(math.log(e["n"]) - math.log(max(1, n))))
     best = e["best"]
     if best == "worklist":
-        return -1, 0, 0
-    b, i, j = best.split("x")
-    return int(b), int(i), int(j)
+        return -1, 0, 0, 0, 0
+    v = [int(x) for x in best.split("x")]
+    if len(v) == 3:
+        v += [256, 4]
+    return tuple(v)

@@ -99,7 +99,8 @@ class Simulation:
     def __init__(self, data, *, G=1.0, ForceSofteningTable=None, TimeStep=0.0, TimeBegin=0.0,
                  TimeEnd=0.1, TimeBase=1 << 30, ErrTolTimestep=0.025, MinStep=1.0e-8,
                  MaxStep=float("inf"), law="spline", precision="mixed", criterion="ref",
-                 device=None, block=0, i_per_thread=0, j_split=0, tuning=None, bgforce=None,
+                 device=None, block=0, i_per_thread=0, j_split=0, tile_j=0, stages=0, tuning=None,
+                 bgforce=None,
                  GravityModel=None, ACC0=0.0, MOND_nuIndex=2.0, TimeIntegrationAlgorithm=None,
                  TimeBetweenSnapshots=None, OutputFunc=None):
         self._lib = L.load()
@@ -146,11 +147,13 @@ class Simulation:
             n0 = np.asarray(data["pos"]).reshape(-1, 3).shape[0]
             shape = autotune.lookup(n0, law=law, path=path)
             if shape:
-                block, i_per_thread, j_split = shape
+                block, i_per_thread, j_split, tile_j, stages = shape
         p.block = int(block)
         p.i_per_thread = int(i_per_thread)
         p.j_split = int(j_split)
-        self.tuned_shape = (int(block), int(i_per_thread), int(j_split))
+        p.tile_j = int(tile_j)
+        p.stages = int(stages)
+        self.tuned_shape = (int(block), int(i_per_thread), int(j_split), int(tile_j), int(stages))
         self.params = p
         alg = TimeIntegrationAlgorithm
         self.euler = alg is Euler or isinstance(alg, Euler) or alg == "Euler"
@@ -343,7 +346,8 @@ def loadrestart(filename, device=None, OutputFunc=None):
                      MinStep=p.min_step, MaxStep=p.max_step, law=inv(LAWS, p.law),
                      precision=inv(PRECISIONS, p.precision), criterion=inv(CRITERIA, p.criterion),
                      device=p.device if device is None else device, block=p.block,
-                     i_per_thread=p.i_per_thread, j_split=p.j_split,
+                     i_per_thread=p.i_per_thread, j_split=p.j_split, tile_j=p.tile_j,
+                     stages=p.stages,
                      TimeIntegrationAlgorithm=Euler if p.algorithm == L.NB_ALG_EULER else Leapfrog,
                      OutputFunc=OutputFunc)
     sim.restore(image)

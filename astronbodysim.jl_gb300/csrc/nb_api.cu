@@ -58,6 +58,8 @@ struct nb_handle {
     float* partial = nullptr;
     size_t partial_bytes = 0;
     int jsplit = 1;
+    int tj = 256;               // sources per packed j-tile (128, 256, 512)
+    int stages = 4;             // depth of the force kernel's copy ring
     int jalloc = 1;             // j-split the arena's partial buffer holds
     float* jpartial = nullptr;  // j-split partials (arena)
     int64_t jstride = 0;
@@ -159,10 +161,14 @@ int check_params(nb_handle* h, const nb_params* p) {
         (p->mond != NB_MOND_MILGROM1983 || !(p->mond_acc0 > 0.0) || !std::isfinite(p->mond_acc0) ||
          !(p->mond_nu_index > 0.0) || !std::isfinite(p->mond_nu_index)))
         return fail(h, NB_ERR_INVALID_ARG, "MOND needs ACC0 > 0 and MOND_nuIndex > 0");
-    if (p->j_split < 0 || p->j_split > 4)
-        return fail(h, NB_ERR_INVALID_ARG, "j_split must be 0..4");
-    if (p->tile_j != 0 && p->tile_j != kTileJ)
-        return fail(h, NB_ERR_INVALID_ARG, "tile_j must be %d", kTileJ);
+    if (p->j_split < 0 || p->j_split > 8)
+        return fail(h, NB_ERR_INVALID_ARG, "j_split must be 0..8");
+    if (p->tile_j != 0 && !nb::tile_size_ok(p->tile_j))
+        return fail(h, NB_ERR_INVALID_ARG, "tile_j must be 0 (auto), 128, 256 or 512");
+    if (p->block == -1 && p->tile_j != 0 && p->tile_j != kTileJ)
+        return fail(h, NB_ERR_INVALID_ARG, "the work-list kernel takes tiles of %d sources", kTileJ);
+    if (p->stages != 0 && p->stages != 3 && p->stages != 4 && p->stages != 6)
+        return fail(h, NB_ERR_INVALID_ARG, "stages must be 0 (auto), 3, 4 or 6");
     if (p->algorithm != NB_ALG_LEAPFROG && p->algorithm != NB_ALG_EULER)
         return fail(h, NB_ERR_INVALID_ARG, "algorithm must be NB_ALG_LEAPFROG or NB_ALG_EULER");
     return NB_OK;
@@ -235,7 +241,7 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     // coordinates relative to its origin stay small.
     e = nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, s);
     if (e != cudaSuccess) return e;
-    e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, kTileJ, h->pack, h->origin, h->ext, s);
+    e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, h->tj, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
     // Built-in choice (the autotuner's result on GB300, Plummer, both laws,
     // N = 2^12 .. 2^20): the direct grid with each i-block's tiles split over
@@ -301,13 +307,14 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
             t2.idx = h->perm;
         }
     }
-    nb::Sources32 src{h->pack, h->origin, h->ext, h->ntiles, kTileJ};
+    nb::Sources32 src{h->pack, h->origin, h->ext, h->ntiles, h->tj};
     if (particles && js > 1 && js <= h->jalloc) {
         src.jsplit = js;
         src.partial = h->jpartial;
         src.pstride = h->jstride;
     }
-    return nb::launch_force_mixed(h->p.law, pot, src, t2, h->p.G, &h->clk->err, blk, ipt, s);
+    return nb::launch_force_mixed(h->p.law, pot, src, t2, h->p.G, &h->clk->err, blk, ipt, s,
+                                  h->stages);
 }
 
 // Force post-processing of the particles that received a force (no-op when
@@ -435,8 +442,10 @@ int ensure_capacity(nb_handle* h, int64_t n) {
         h->arena = nullptr;
         h->cap = 0;
     }
-    const int64_t ntiles = (n + kTileJ - 1) / kTileJ;
-    const int64_t npad = ntiles * kTileJ;
+    // room for every tile size: tile records for tiles of 128, padded sources
+    // for tiles of 512
+    const int64_t ntiles = (n + 127) / 128;
+    const int64_t npad = (n + 511) / 512 * 512;
     const int64_t dblocks = nb::diag_scratch_doubles(n);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -494,7 +503,7 @@ int ensure_capacity(nb_handle* h, int64_t n) {
     h->diag_scratch = (double*)(b + o_ds);
     h->diag_blocks = dblocks / 8;
     h->diag_out = (double*)(b + o_do);
-    h->ntiles = (int32_t)ntiles;
+    h->ntiles = (int32_t)((n + h->tj - 1) / h->tj);
     return NB_OK;
 }
 
@@ -519,6 +528,8 @@ void apply_tuning(nb_handle* h, const nb_params& p) {
     h->block = p.block > 0 ? p.block : 128;
     h->ipt = p.i_per_thread ? p.i_per_thread : 2;
     h->jsplit = p.j_split > 1 ? p.j_split : 1;
+    h->tj = p.tile_j ? p.tile_j : kTileJ;
+    h->stages = p.stages ? p.stages : 4;
     h->worklist = p.block == -1;
     h->auto_cfg = p.block == 0 && p.i_per_thread == 0;
 }
@@ -692,7 +703,7 @@ int nb_upload(nb_handle* h, int64_t n, const double* x, const double* y, const d
     }
     h->n = n;
     // tiles of this upload (the arena may hold more from a larger earlier one)
-    h->ntiles = (int32_t)((n + kTileJ - 1) / kTileJ);
+    h->ntiles = (int32_t)((n + h->tj - 1) / h->tj);
     drop_graph(h);
     if (n == 0) return NB_OK;
     const size_t d = sizeof(double) * (size_t)n;
@@ -1264,7 +1275,7 @@ int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
         if (rc) return rc;
     }
     h->n = n;
-    h->ntiles = (int32_t)((n + kTileJ - 1) / kTileJ);
+    h->ntiles = (int32_t)((n + h->tj - 1) / h->tj);
     NB_CK(cudaMemcpy(h->clk, &hd.clk, sizeof(Clock), cudaMemcpyHostToDevice));
     if (n == 0) return NB_OK;
     size_t off = sizeof hd;

@@ -1,0 +1,13 @@
+// nb_force_mixed_t128.cu -- the mixed-precision force kernels with j-tiles of
+// 128 sources (one translation unit per tile size, compiled in parallel).
+#include "nb_force_mixed.cuh"
+
+namespace nb {
+
+template cudaError_t launch_force_mixed_tile<128>(int, bool, const Sources32&, const Targets&, double,
+                                                 uint32_t*, int, int, int, cudaStream_t);
+template cudaError_t launch_pack_tile<128>(const double*, const double*, const double*,
+                                          const double*, int64_t, const int32_t*, float4*,
+                                          TileOrigin*, float4*, cudaStream_t);
+
+}  // namespace nb

@@ -265,8 +265,13 @@ cudaError_t launch_morton_sort(const double* x, const double* y, const double* z
                                void* scratch, int32_t* perm, cudaStream_t s);
 uint64_t* sort_keys_buffer(void* scratch, int64_t n);
 cudaError_t launch_sort_keys(void* scratch, int64_t n, int32_t* vals, int passes, cudaStream_t s);
+// Tile sizes of the packed sources: 128, 256 or 512 (src.tile_j); stages:
+// depth of the force kernel's shared-memory ring (3, 4, 6; see
+// nb_force_mixed.cuh for the combinations compiled).
 cudaError_t launch_force_mixed(int law, bool pot, const Sources32& src, const Targets& tg,
-                               double G, uint32_t* err, int block, int ipt, cudaStream_t s);
+                               double G, uint32_t* err, int block, int ipt, cudaStream_t s,
+                               int stages = 4);
+bool tile_size_ok(int tile_j);
 cudaError_t launch_force_fp64(int law, bool pot, const Sources64& src, const Targets& tg,
                               double G, uint32_t* err, cudaStream_t s);
 

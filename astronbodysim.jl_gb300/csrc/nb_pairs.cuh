@@ -92,7 +92,7 @@ __device__ __forceinline__ bool warp_near(const float4 e, const float* xr, const
 // interaction).  Zero-mass padding (at 1e18) then adds r^-3 = 0 exactly to
 // the acceleration (the product underflows) but 1e-18 per slot to the
 // potential, so partial tiles take this form only without the potential.
-template <int LAW, bool ACC, bool POT, int IPT, bool UNI = false>
+template <int LAW, bool ACC, bool POT, int IPT, bool UNI = false, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, const float* xr,
                                                const float* yr, const float* zr, const float* h2,
                                                float* ax, float* ay, float* az, float* ap,
@@ -113,7 +113,7 @@ __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, con
         for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
 #pragma unroll (LoopShape<IPT>::UNROLL)
-    for (int p = 0; p < kTileJ / 2; p += NA) {
+    for (int p = 0; p < TJ / 2; p += NA) {
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
             const float4 A = b[2 * (p + u)];
@@ -193,7 +193,7 @@ __device__ __forceinline__ bool warp_expandable(float radius, const float* xr, c
     return __all_sync(0xffffffffu, ok);
 }
 
-template <int LAW, bool ACC, bool POT, int IPT>
+template <int LAW, bool ACC, bool POT, int IPT, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_expand(const float4* __restrict__ b, const float* xr,
                                                  const float* yr, const float* zr,
                                                  const float* h2, float* ax, float* ay, float* az,
@@ -214,7 +214,7 @@ __device__ __forceinline__ void pair_loop_expand(const float4* __restrict__ b, c
             sx[u][k] = sy[u][k] = sz[u][k] = sw[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
 #pragma unroll (LoopShape<IPT>::UNROLL)
-    for (int p = 0; p < kTileJ / 2; p += NA) {
+    for (int p = 0; p < TJ / 2; p += NA) {
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
             const float4 A = b[2 * (p + u)];
@@ -258,19 +258,19 @@ __device__ __forceinline__ void pair_loop_expand(const float4* __restrict__ b, c
 }
 
 // Far-tile dispatch: the uniform-mass loop when the pack flagged the tile.
-template <int LAW, bool ACC, bool POT, int IPT>
+template <int LAW, bool ACC, bool POT, int IPT, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_far(const float4* __restrict__ b, const float* xr,
                                               const float* yr, const float* zr, const float* h2,
                                               float* ax, float* ay, float* az, float* ap, float mu) {
     // mu < 0: uniform but partial tile (usable for the acceleration only)
     const float m = POT ? mu : fabsf(mu);
     if (m > 0.0f)
-        pair_loop_fast<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, h2, ax, ay, az, ap, m);
+        pair_loop_fast<LAW, ACC, POT, IPT, true, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap, m);
     else
-        pair_loop_fast<LAW, ACC, POT, IPT, false>(b, xr, yr, zr, h2, ax, ay, az, ap);
+        pair_loop_fast<LAW, ACC, POT, IPT, false, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap);
 }
 
-template <int LAW, bool ACC, bool POT, int IPT, bool UNI>
+template <int LAW, bool ACC, bool POT, int IPT, bool UNI, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict__ b, const float* xr,
                                                        const float* yr, const float* zr,
                                                        const float* hh, const float* h2, float* ax,
@@ -295,7 +295,7 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
         for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
 #pragma unroll (LoopShape<IPT>::UNROLL)
-    for (int p = 0; p < kTileJ / 2; p += NA) {
+    for (int p = 0; p < TJ / 2; p += NA) {
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
             const float4 A = b[2 * (p + u)];
@@ -397,16 +397,16 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
 }
 
 // Near-tile loop: the uniform-mass form when the pack flagged the tile.
-template <int LAW, bool ACC, bool POT, int IPT>
+template <int LAW, bool ACC, bool POT, int IPT, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, const float* xr,
                                                   const float* yr, const float* zr,
                                                   const float* hh, const float* h2, float* ax,
                                                   float* ay, float* az, float* ap, float mu) {
     const float m = POT ? mu : fabsf(mu);
     if (m > 0.0f)
-        pair_loop_checked_impl<LAW, ACC, POT, IPT, true>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, m);
+        pair_loop_checked_impl<LAW, ACC, POT, IPT, true, TJ>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, m);
     else
-        pair_loop_checked_impl<LAW, ACC, POT, IPT, false>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, 1.0f);
+        pair_loop_checked_impl<LAW, ACC, POT, IPT, false, TJ>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, 1.0f);
 }
 
 }  // namespace nb

@@ -68,12 +68,12 @@ typedef struct nb_params {
     double time_begin;    /* TimeBegin */
     double time_end;      /* TimeEnd; TimeInterval = (end-begin)/time_base */
     int32_t device;       /* CUDA ordinal */
-    int32_t tile_j;       /* tuning override: j-tile (0 = auto) */
+    int32_t tile_j;       /* tuning override: sources per j-tile, 128, 256 or 512 (0 = 256) */
     int32_t i_per_thread; /* tuning override (0 = auto) */
     int32_t block;        /* tuning override: threads per CTA of the direct grid (128, 256);
                              -1 = persistent work-list kernel; 0 (with i_per_thread 0) = auto */
     int32_t j_split;      /* tuning override: CTAs sharing one i-block's sources in the direct
-                             grid (1..4; 0 = 1) */
+                             grid (1..8; 0 = 1) */
     int32_t algorithm;    /* NB_ALG_LEAPFROG (default) or NB_ALG_EULER: whether nb_run_begin /
                              nb_run_end apply the half kicks; kept in checkpoint images */
     /* Force post-processing, applied by nb_compute_force and nb_step to the
@@ -91,6 +91,9 @@ typedef struct nb_params {
     double bg_rg;         /* gravity radius r_g of NB_BG_PSEUDO_NEWTONIAN */
     double mond_acc0;     /* ACC0 (> 0 when mond is set) */
     double mond_nu_index; /* MOND_nuIndex (reference default 2) */
+    int32_t stages;       /* tuning override: depth of the force kernel's shared-memory ring of
+                             j-tiles, 3, 4 or 6 (0 = 4) */
+    int32_t reserved;
 } nb_params;
 
 #define NB_BG_NONE 0

@@ -353,7 +353,10 @@ def test_builtin_rule_at_large_n_matches_explicit_shape_and_oracle(nb, oracle):
     nb.compute_force(a)
     np.testing.assert_array_equal(ga, nb.get_all_data(a)["acc"])
     nb.compute_force(b)
-    assert rel_err(ga, nb.get_all_data(b)["acc"]).max() <= 1e-6
+    # two mixed forms (two targets per thread with the j-split against one
+    # target per thread unsplit) differ by their own FP32 round-off
+    er = rel_err(ga, nb.get_all_data(b)["acc"])
+    assert np.median(er) <= 1e-7 and er.max() <= 1e-5
     sub = np.arange(0, n, 512)
     a_ref, _ = oracle.force(d["pos"], d["mass"], d["pos"][sub], h)
     e = rel_err(ga[sub], a_ref)
