@@ -127,6 +127,157 @@ def cpu_oracle_rate(data, n_targets, seed=7, nthreads=0):
     return n_targets * data["pos"].shape[0] / dt, dt, oracle.max_threads() if nthreads == 0 else nthreads
 
 
+def measured_fp32_peak(device):
+    """FP32 FMA throughput measured on this GPU (nb_selftest_fp32_peak:
+    independent fma.rn.f32x2 chains, CUDA events), TFLOP/s at 2 flop per lane."""
+    import ctypes
+
+    from astronbodysim import _lib as L
+
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    rc = L.load().nb_selftest_fp32_peak(int(device), 1, ctypes.byref(tf), ctypes.byref(ms))
+    if rc != 0:
+        return None
+    return tf.value
+
+
+def timed_forces(nb, sim, stream, flush, reps):
+    """CUDA-event times (ms) of `reps` nb_compute_force calls on the handle's
+    stream, each after an L2 flush outside the events."""
+    import torch
+
+    ev = []
+    for _ in range(reps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        nb.compute_force(sim)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        ev.append((e0, e1))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def general_mass_leg(nb, data, args, local, stream, flush, oracle_targets=1024):
+    """The same Plummer positions with masses m (1 + d_i), d_i ~ U[-1e-3, 1e-3]
+    (seeded), so that no tile has one common mass: force throughput (CUDA
+    events) and relative force errors against the oracle."""
+    from oracle import oracle
+
+    n = data["pos"].shape[0]
+    rng = np.random.default_rng(77)
+    d = {"pos": data["pos"], "vel": data["vel"],
+         "mass": data["mass"] * (1.0 + rng.uniform(-1e-3, 1e-3, size=n))}
+    sim = nb.Simulation(d, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
+                        precision="mixed", law=args.law, device=local, tuning="auto")
+    sim.set_stream(stream.cuda_stream)
+    nb.compute_force(sim)
+    ms = statistics.median(timed_forces(nb, sim, stream, flush, 3))
+    sub = np.sort(rng.choice(n, size=oracle_targets, replace=False))
+    g = nb.get_all_data(sim)
+    a_ref, _ = oracle.force(d["pos"], d["mass"], d["pos"][sub], EPS, want_pot=False,
+                            law=oracle.LAW_SPLINE_G2 if args.law == "spline" else oracle.LAW_PLUMMER)
+    e = np.linalg.norm(g["acc"][sub] - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+    sim.close()
+    return {"value": float(n) * n / (ms / 1e3) / 1e9, "unit": UNIT, "force_ms": ms,
+            "masses": "m_i = (1/N)(1 + d_i), d_i ~ U[-1e-3, 1e-3]",
+            "force_rel_median": float(np.median(e)), "force_rel_p99": float(np.quantile(e, 0.99)),
+            "force_rel_max": float(e.max()), "error_targets": oracle_targets}
+
+
+def fp64_leg(nb, data, args, local, stream, n_targets):
+    """Plain FP64 form at full occupancy: acceleration only at n_targets
+    seeded particles (probe points) from all N sources, one launch of
+    k_force_fp64 timed with CUDA events around the call on the handle's
+    stream (the call also copies the n_targets positions in and the
+    accelerations out, 48 B per target)."""
+    import ctypes
+
+    import torch
+
+    from astronbodysim import _lib as L
+    from oracle import oracle
+
+    n = data["pos"].shape[0]
+    rng = np.random.default_rng(78)
+    sub = np.sort(rng.choice(n, size=n_targets, replace=False))
+    sim = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
+                        precision="fp64", law=args.law, device=local)
+    sim.set_stream(stream.cuda_stream)
+    p = data["pos"][sub]
+    cols = [np.ascontiguousarray(p[:, k]) for k in range(3)]
+    out = [np.empty(n_targets) for _ in range(3)]
+    lib = sim._lib
+    nullp = ctypes.POINTER(ctypes.c_double)()
+
+    def call(m):
+        sim._ck(lib.nb_force_at_points(sim.handle, m, *[L.dptr(c) for c in cols], EPS,
+                                       *[L.dptr(o) for o in out], nullp))
+
+    call(1024)  # warm-up
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    call(n_targets)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    k = 256
+    a_ref, _ = oracle.force(data["pos"], data["mass"], p[:k], EPS, want_pot=False,
+                            law=oracle.LAW_SPLINE_G2 if args.law == "spline" else oracle.LAW_PLUMMER)
+    a = np.stack([o[:k] for o in out], 1)
+    e = np.linalg.norm(a - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
+    sim.close()
+    return {"value": float(n_targets) * n / (ms / 1e3) / 1e9, "unit": UNIT, "ms": ms,
+            "sample": "%d targets x %d sources, acceleration only, one launch (%d CTAs of 128)"
+                      % (n_targets, n, (n_targets + 127) // 128),
+            "force_rel_max_256": float(e.max())}
+
+
+def relaunch_replicas(gpus):
+    """`bench.py --gpus N` started as one process: run it again as N replica
+    processes (one per GPU) under torch.distributed.run on this node, and
+    return their exit status.  Rank 0 prints the job's JSON line."""
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           "--nproc-per-node", str(gpus), "--master-addr", "127.0.0.1", "--master-port", str(port),
+           os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
+def run_dry(args):
+    """Launcher and aggregation check without a GPU: every rank (gloo) times
+    a fixed host workload that takes rank + 1 units of 50 ms as its "steps",
+    then the job time is the MAX over ranks and rank 0 prints the JSON line
+    with n_gpus = world size, as the GPU bench does."""
+    import torch.distributed as dist
+
+    ws, rank, _ = dist_env()
+    if ws > 1:
+        dist.init_process_group("gloo")
+        dist.barrier()
+    t0 = time.perf_counter()
+    time.sleep(0.05 * (rank + 1))
+    total_s = time.perf_counter() - t0
+    n = 1024
+    value, e2e, total_s, _ = replica_rates(ws, args.steps, args.steps, n, total_s, total_s, None)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+                          "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": 1e3 * total_s / args.steps, "dry_run": True,
+                          "scaling": "weak"}), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
 def replica_rates(ws, steps, e2e_steps, n, total_s, t_e2e, device):
     """Whole-job rates of ws independent replicas (one system of n particles
     per rank, no data-path collective): the job time is the slowest rank's
@@ -191,7 +342,7 @@ def run_gpu(args):
     data = nb.plummer(n, seed=2 + rank)
     sim = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
                         precision="mixed", law=args.law, device=local, block=args.block,
-                        i_per_thread=args.ipt, j_split=args.jsplit,
+                        i_per_thread=args.ipt, j_split=args.jsplit, tile_j=args.tile, stages=args.stages,
                         tuning=None if (args.block or args.ipt or args.jsplit) else "auto")
     tuned = sim.tuned_shape
     stream = torch.cuda.Stream(device=dev)
@@ -219,15 +370,10 @@ def run_gpu(args):
         # plain FP64 form on the same targets (probe points at the particles)
         sim64 = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
                               precision="fp64", law=args.law, device=local)
-        nb.force_and_potential_at_points(sim64, data["pos"][sub[:256]], EPS)  # warm-up
-        t0 = time.perf_counter()
         a64, p64 = nb.force_and_potential_at_points(sim64, data["pos"][sub], EPS)
-        t64 = time.perf_counter() - t0
         e64 = np.linalg.norm(a64 - a_ref, axis=1) / np.linalg.norm(a_ref, axis=1)
         ep64 = np.abs(p64 - p_ref) / np.abs(p_ref)
-        acc_stats["fp64"] = {"force_rel_max": float(e64.max()), "pot_rel_max": float(ep64.max()),
-                             "g_interactions_per_s_force_and_potential": len(sub) * n / t64 / 1e9,
-                             "sample": "%d targets x %d sources, force+potential, host timer" % (len(sub), n)}
+        acc_stats["fp64"] = {"force_rel_max": float(e64.max()), "pot_rel_max": float(ep64.max())}
         sim64.close()
         acc_stats["targets"] = int(len(sub))
 
@@ -288,6 +434,13 @@ def run_gpu(args):
             "momentum_abs_drift": float(np.linalg.norm(d1["P"] - d0["P"]))}
         acc_stats["energy_drift_mixed_vs_fp64_n32768"] = energy_drift_pair(nb, args.law, local)
 
+    # ---- general masses and the plain FP64 form (throughput legs) ----------
+    extra = {}
+    if rank == 0 and not args.skip_accuracy:
+        extra["general_mass"] = general_mass_leg(nb, data, args, local, stream, flush)
+        extra["fp64_plain"] = fp64_leg(nb, data, args, local, stream, args.fp64_targets)
+        extra["fp64_plain"]["mixed_over_fp64"] = (n * n / (force_ms / 1e3) / 1e9) / extra["fp64_plain"]["value"]
+
     # ---- end to end through the public API with host buffers ---------------
     pin = {k: torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
            for k in ("x", "y", "z", "vx", "vy", "vz", "ax", "ay", "az", "m")}
@@ -340,15 +493,21 @@ def run_gpu(args):
         peaks = measured_peaks()
         props = torch.cuda.get_device_properties(dev)
         sm_max = peaks.get("sm_max_mhz") or clocks.get("sm_max_mhz") or 2070.0
-        fp32_peak_tflops = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+        nominal_tflops = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+        fp32_measured = measured_fp32_peak(local)
+        fp32_peak_tflops = fp32_measured or nominal_tflops
         achieved = FLOP_PER_INTERACTION * pairs / (force_ms / 1e3) / 1e12
+        # the launch shape the handle used (built-in rule when no table entry)
+        tuned_eff = tuned if tuned[:2] != (0, 0) else (128, 2 if n >= (1 << 16) else 1, 4, 0, 0)
+        tuned_eff = tuple(tuned_eff[:3]) + (tuned_eff[3] or 256, tuned_eff[4] or 4)
         traffic = None
         tpath = os.path.join(REPO, "profiles", "force_mixed_traffic.json")
         if os.path.exists(tpath):
             try:
                 with open(tpath) as f:
                     tj = json.load(f)
-                traffic = tj.get("bytes_per_launch_scaled_to_n%d" % n)
+                if tj.get("shape") == "%dx%dx%dx%dx%d" % tuned_eff:
+                    traffic = tj.get("bytes_per_launch_scaled_to_n%d" % n)
             except Exception:
                 traffic = None
         cpu = None
@@ -367,22 +526,28 @@ def run_gpu(args):
                        "step": "drift+pack+force(N^2)+kick, one CUDA graph replay",
                        "l2": "256 MiB write between timed steps, outside the events",
                        "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "force_kernel": ("block=%d i_per_thread=%d j_split=%d (%s)" % (
-                           tuned[0], tuned[1], tuned[2],
-                           "explicit" if (args.block or args.ipt or args.jsplit) else
-                           ("autotuner table" if tuned[:2] != (0, 0) else
-                            "built-in rule: direct 128x1 for N >= 2^19, work list below")))},
+                       "force_kernel": ("block=%d i_per_thread=%d j_split=%d tile=%d stages=%d (%s)" % (
+                           tuned_eff + ("explicit" if (args.block or args.ipt or args.jsplit) else
+                                        ("autotuner table" if tuned[:2] != (0, 0) else
+                                         "built-in rule of the library"),)))},
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak_tflops,
                          "unit": "TFLOP/s", "frac": achieved / fp32_peak_tflops, "traffic": traffic,
-                         "kernel": "k_force_mixed (+k_pack)", "force_ms": force_ms,
-                         "peak_note": "FP32 peak = SMs x 128 lanes x 2 x sm_max_mhz (%s); 20 flop/interaction"
-                                      % ("MEASURED_PEAKS.json" if peaks.get("sm_max_mhz") else "nvidia-smi")},
+                         "kernel": "k_force_mixed (+k_pack, k_force_join)", "force_ms": force_ms,
+                         "peak_note": ("of measured: fma.rn.f32x2 throughput of this GPU (nb_selftest_fp32_peak); "
+                                       "nominal SMs x 128 lanes x 2 x %.0f MHz = %.1f TFLOP/s; 20 flop/interaction"
+                                       % (sm_max, nominal_tflops)) if fp32_measured else
+                                      "of nominal: SMs x 128 lanes x 2 x sm_max_mhz; 20 flop/interaction",
+                         "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of "
+                                         "this launch shape at N = 2^18, scaled by N (profiles/force_mixed_traffic.json); "
+                                         "null when the file names another shape"},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": args.e2e_steps},
-            "gpu_launches": (STEP_KERNELS + (1 if tuned[2] > 1 or tuned[0] == -1 else 0)) * args.steps,
+            "gpu_launches": (STEP_KERNELS + (1 if tuned_eff[2] > 1 or tuned_eff[0] == -1 else 0)) * args.steps,
             "clocks": clocks,
             "accuracy": acc_stats,
+            "general_mass": extra.get("general_mass"),
+            "fp64_plain": extra.get("fp64_plain"),
             "batch": batch,
             "serve": serve_stats,
             "wall_s_timed": t_wall,
@@ -570,8 +735,11 @@ def main():
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--ipt", type=int, default=0)
     ap.add_argument("--jsplit", type=int, default=0)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--stages", type=int, default=0)
     ap.add_argument("--force-reps", type=int, default=3)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--fp64-targets", type=int, default=152 * 128 * 4)
     ap.add_argument("--acc-targets", type=int, default=4096)
     ap.add_argument("--cpu-targets", type=int, default=2048)
     ap.add_argument("--ref-targets", type=int, default=1024)
@@ -591,7 +759,17 @@ def main():
     ap.add_argument("--n-each", type=int, default=1 << 20)
     ap.add_argument("--base-steps", type=int, default=2)
     ap.add_argument("--fp64-compare", action="store_true")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="check the replica launcher and max-over-ranks aggregation on the host (no GPU)")
     args = ap.parse_args()
+    world = os.environ.get("WORLD_SIZE")
+    if args.gpus > 1 and world is None:
+        return relaunch_replicas(args.gpus)
+    if world is not None and int(world) != args.gpus:
+        print("bench.py: --gpus %d but WORLD_SIZE=%s" % (args.gpus, world), file=sys.stderr)
+        return 2
+    if args.dry_run:
+        return run_dry(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.mode == "serve":
