@@ -317,6 +317,9 @@ __global__ void __launch_bounds__(kTileJ)
         qz = rel_df(split_df(pz), to.hi.z, to.lo.z);
         qm = (float)pm;
     }
+    // A full tile of one common mass keeps that mass in ext.w only; its mass
+    // slots hold |q|^2 for the expanded far loop (pair_loop_expand).
+    if (uniform && (t + 1) * kTileJ <= d.n) qm = fmaf(qx, qx, fmaf(qy, qy, qz * qz));
     float* base = reinterpret_cast<float*>(pack + (int64_t)g * kTileJ);
     const int pr = threadIdx.x >> 1, half = threadIdx.x & 1;
     base[8 * pr + half] = qx;
@@ -355,8 +358,17 @@ __global__ void __launch_bounds__(kTileJ)
 // Launch shapes (threads per CTA, targets per thread); an item is one i-block
 // of BLOCK * IPT targets.  Default 128 x 2; the engine takes the shape from its
 // parameters (chosen by the autotuner).
+// Register budget: acceleration-only launches of 128 threads are held to 6
+// (one target per thread) or 5 (two) CTAs per SM, the counts at which the
+// pair loop compiles without spills (as the single-system kernel).
+template <int BLOCK, int IPT, bool ACC, bool POT>
+struct BatchOcc {
+    static constexpr int value =
+        (ACC && !POT) ? (BLOCK == 128 ? (IPT == 1 ? 6 : 5) : (IPT == 1 ? 3 : 2)) : 1;
+};
+
 template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) : 1)
+__global__ void __launch_bounds__(BLOCK, (BatchOcc<BLOCK, IPT, ACC, POT>::value))
     k_force_batch(BatchForce f) {
     constexpr int NW = BLOCK / 32;
     constexpr int kFBt = BLOCK * IPT;
@@ -450,13 +462,15 @@ __global__ void __launch_bounds__(BLOCK, (ACC && !POT) ? (BLOCK == 128 ? 8 : 4) 
                 break;
             }
             const float4* b = &buf[st * kTileJ];
+            const float4 ex = f.ext[d.tile_off + t];
             bool near = false;
-            if (LAW == NB_LAW_SPLINE_G2)
-                near = warp_near<IPT>(f.ext[d.tile_off + t], xr, yr, zr, hh, pidx);
+            if (LAW == NB_LAW_SPLINE_G2) near = warp_near<IPT>(ex, xr, yr, zr, hh, pidx);
             if (near)
-                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, f.ext[d.tile_off + t].w);
+                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, ex.w);
+            else if (ex.w > 0.0f && warp_expandable<IPT>(oh.w, xr, yr, zr, pidx))
+                pair_loop_expand<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);
             else
-                pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, f.ext[d.tile_off + t].w);
+                pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);
             __syncwarp();
             if (lane == 0) {
                 __threadfence_block();
