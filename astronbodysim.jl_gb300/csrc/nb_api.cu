@@ -69,12 +69,19 @@ struct nb_handle {
 namespace {
 
 constexpr int kTileJ = 256;
-// Built-in launch rule (the autotuner's choice on GB300, both laws): the
-// direct grid of 128-thread CTAs with each i-block's tiles split over 4 CTAs,
-// one target per thread below 2^16 particles and two from 2^16 on (N = 2^20:
-// 351 ms against 367 ms per force).
-constexpr int kAutoJsplit = 4;
+// Built-in launch rule (the autotuner's choices on GB300, both laws, rounded
+// to three size classes): the direct grid of 128-thread CTAs with each
+// i-block's tiles split over several CTAs --
+//   N <  2^16: one target per thread, j-split 4, tiles of 256;
+//   N >= 2^16: two targets per thread, j-split 8, tiles of 256;
+//   N >= 2^17: the same with tiles of 512 (N = 2^20: 345 ms per force against
+//              367 ms for the first rule).
+constexpr int kAutoJsplitMax = 8;
 constexpr int64_t kAutoIpt2From = 1 << 16;
+constexpr int64_t kAutoTile512From = 1 << 17;
+
+int auto_jsplit(int64_t n) { return n >= kAutoIpt2From ? 8 : 4; }
+int auto_tile(int64_t n) { return n >= kAutoTile512From ? 512 : 256; }
 
 int fail(nb_handle* h, int code, const char* fmt, ...) {
     if (h) {
@@ -243,11 +250,11 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     if (e != cudaSuccess) return e;
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, h->tj, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
-    // Built-in choice (the autotuner's result on GB300, Plummer, both laws,
-    // N = 2^12 .. 2^20): the direct grid with each i-block's tiles split over
-    // 4 CTAs, whose compensated partials are joined in order, and two targets
-    // per thread from 2^16 particles on.  The split keeps the grid several
-    // waves deep at small N, where the work list was used before.
+    // Built-in choice (the size classes of kAutoIpt2From / kAutoTile512From
+    // above): the direct grid with each i-block's tiles split over 4 or 8
+    // CTAs, whose compensated partials are joined in order.  The split keeps
+    // the grid several waves deep at small N and its last wave short at large
+    // N.
     bool use_wl = h->worklist;
     int blk = h->block, ipt = h->ipt;
     int js = h->jsplit;
@@ -255,7 +262,7 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
         use_wl = false;
         blk = 128;
         ipt = h->n >= kAutoIpt2From ? 2 : 1;
-        js = kAutoJsplit;
+        js = auto_jsplit(h->n);
     }
     if (particles && use_wl) {
         if (active_only) {
@@ -434,7 +441,7 @@ cudaError_t capture_output_graph(nb_handle* h, cudaGraphExec_t* out) {
 }
 
 int ensure_capacity(nb_handle* h, int64_t n) {
-    const int js_need = h->auto_cfg ? kAutoJsplit : h->jsplit;
+    const int js_need = h->auto_cfg ? kAutoJsplitMax : h->jsplit;
     if (n <= h->cap && h->arena && js_need <= h->jalloc) return NB_OK;
     drop_graph(h);
     if (h->arena) {
@@ -698,6 +705,7 @@ int nb_upload(nb_handle* h, int64_t n, const double* x, const double* y, const d
     int rc = use_device(h);
     if (rc) return rc;
     if (n > 0) {
+        if (h->auto_cfg && h->p.tile_j == 0) h->tj = auto_tile(n);
         rc = ensure_capacity(h, n);
         if (rc) return rc;
     }
@@ -1271,6 +1279,7 @@ int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
     apply_tuning(h, p);
     // ensure_capacity re-lays the arena out when the j-split needs more room
     if (n > 0) {
+        if (h->auto_cfg && h->p.tile_j == 0) h->tj = auto_tile(n);
         rc = ensure_capacity(h, n);
         if (rc) return rc;
     }
