@@ -19,7 +19,11 @@
 //     race on it and corrupt each other's results -- serialise them.
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress while that device is current and caches it; that first
-// call should come before any stream capture.
+// call should come before any stream capture.  Later calls check the cached
+// address with cudaPointerGetAttributes (no allocation) and repeat the set-up
+// when it no longer names device memory of the current device -- after a
+// cudaDeviceReset, which ends the context the address belonged to.  Every
+// call synchronises its stream before it returns.
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -61,6 +65,17 @@ void set_msg(char* buf, int64_t len, const char* msg) {
     std::snprintf(buf, (size_t)len, "nb_force_noalloc: %s", msg);
 }
 
+// True when p still names device memory of device dev (the cached scratch
+// address of a context that has not been reset).
+bool still_valid(const void* p, int dev) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();  // clear the error the failed query recorded
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
+}
+
 // Device address of the shared scratch on the current device (set-up on first use).
 cudaError_t scratch_address(void** out) {
     int dev = 0;
@@ -68,6 +83,7 @@ cudaError_t scratch_address(void** out) {
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_mu);
+    if (g_scratch_addr[dev] && !still_valid(g_scratch_addr[dev], dev)) g_scratch_addr[dev] = nullptr;
     if (!g_scratch_addr[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);

@@ -285,8 +285,10 @@ int nb_checkpoint_load(nb_handle *h, const void *buf, int64_t bytes);
  * errbuf (may be NULL).  All calls share that array: calls that overlap on the
  * GPU race and must be serialised by the caller.  The first call on a device
  * looks up the array's address and should come before any stream capture.
- * Results equal nb_compute_force of a handle with NB_PREC_MIXED, the same law,
- * G and softening for every particle type. */
+ * Results agree with nb_compute_force of a handle with NB_PREC_MIXED, the same
+ * law, G and softening for every particle type, within the mixed-precision
+ * tolerance: the same kernels, with another launch shape (128 threads x 2
+ * targets, no j-split), so the FP32 sums run in another order. */
 int nb_force_noalloc(int64_t n, const double *x, const double *y, const double *z,
                      const double *m, int32_t law, double G, double softening, double *ax,
                      double *ay, double *az, double *pot, void *stream, char *errbuf,

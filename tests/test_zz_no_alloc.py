@@ -7,9 +7,12 @@ The caller's device arrays come from torch here.  The entry point is compared
 with the handle path (nb_compute_force, mixed precision) on two calls in a row;
 the two calls share the library's fixed scratch array, so the second call also
 checks that nothing left over from the first one leaks into its result.  The
-tolerance is the mixed-precision force tolerance of the other GPU tests
-(relative 1e-5 per particle); the two paths run the same kernels, so the
-results normally agree bit for bit.
+handle path runs the same kernels with another launch shape, so the FP32 sums
+differ in order: the tolerance is the mixed-precision bar of the other GPU
+tests (relative force and potential error: median <= 1e-6, p99 <= 1e-5,
+max <= 1e-4).  Sizes: one particle, a partial tile, a mid size and the
+maximum; with and without the potential.  A warm call must leave the device's
+free memory unchanged.
 """
 import ctypes
 
@@ -35,14 +38,22 @@ def _call(lib, torch, n, cols, law, G, h, outs, want_pot=True):
     return rc, buf.value.decode()
 
 
+def _within_bar(got, ref):
+    e = np.abs(got - ref) / np.maximum(np.abs(ref), 1e-300)
+    return np.median(e) <= 1e-6 and np.quantile(e, 0.99) <= 1e-5 and e.max() <= 1e-4
+
+
 @pytest.mark.parametrize("law", ["spline", "plummer"])
-def test_noalloc_matches_handle_path_twice(nb, law):
+@pytest.mark.parametrize("n", [1, 257, 20000, MAX_PARTICLES])
+@pytest.mark.parametrize("want_pot", [True, False])
+def test_noalloc_matches_handle_path_twice(nb, law, n, want_pot):
     torch = pytest.importorskip("torch")
     from astronbodysim import _lib as L
 
     lib = L.load()
-    n, h, G = 20000, 0.01, 1.5
-    d = nb.plummer(n, seed=21)
+    h, G = 0.01, 1.5
+    d = nb.plummer(n, seed=21) if n > 1 else {"pos": np.array([[0.3, -0.2, 0.1]]),
+                                              "vel": np.zeros((1, 3)), "mass": np.ones(1)}
     sim = nb.Simulation(d, G=G, ForceSofteningTable=[h] * 6, TimeStep=1e-3, precision="mixed",
                         law=law)
     nb.compute_force(sim, want_potential=True)
@@ -51,16 +62,31 @@ def test_noalloc_matches_handle_path_twice(nb, law):
     ilaw = L.NB_LAW_SPLINE_G2 if law == "spline" else L.NB_LAW_PLUMMER
     for call in range(2):
         outs = [torch.full((n,), float("nan"), dtype=torch.float64, device="cuda:0") for _ in range(4)]
-        rc, msg = _call(lib, torch, n, cols, ilaw, G, h, outs)
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        rc, msg = _call(lib, torch, n, cols, ilaw, G, h, outs, want_pot)
         assert rc == L.NB_OK, msg
         torch.cuda.synchronize()
+        if call == 1:
+            # the warm call takes no device memory
+            assert torch.cuda.mem_get_info()[0] == free0
         acc = torch.stack(outs[:3], 1).cpu().numpy()
+        assert np.all(np.isfinite(acc)), call
+        if n == 1:
+            assert np.all(acc == 0.0) and np.all(ref["acc"] == 0.0)
+        else:
+            na = np.linalg.norm(acc - ref["acc"], axis=1)
+            e = na / np.linalg.norm(ref["acc"], axis=1)
+            assert np.median(e) <= 1e-6 and np.quantile(e, 0.99) <= 1e-5 and e.max() <= 1e-4, call
         pot = outs[3].cpu().numpy()
-        e = np.linalg.norm(acc - ref["acc"], axis=1) / np.linalg.norm(ref["acc"], axis=1)
-        ep = np.abs(pot - ref["pot"]) / np.abs(ref["pot"])
-        assert np.all(np.isfinite(acc)) and np.all(np.isfinite(pot)), call
-        assert e.max() <= 1e-5, (call, e.max())
-        assert ep.max() <= 1e-5, (call, ep.max())
+        if want_pot:
+            assert np.all(np.isfinite(pot)), call
+            if n == 1:
+                assert pot[0] == ref["pot"][0]
+            else:
+                assert _within_bar(pot, ref["pot"]), call
+        else:
+            assert np.all(np.isnan(pot)), "pot must stay untouched without a potential"
 
 
 def test_noalloc_rejects_sizes_beyond_maximum(nb):
