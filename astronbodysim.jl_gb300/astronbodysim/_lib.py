@@ -179,6 +179,8 @@ SIGNATURES = {
     "nb_batch_submit": (ctypes.c_int, [_h, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                                        ctypes.c_double, ctypes.c_double, ctypes.c_int64, _i64p]),
     "nb_engine_run": (ctypes.c_int, [_h, ctypes.c_int64, _i64p]),
+    "nb_engine_run_async": (ctypes.c_int, [_h, ctypes.c_int64, _i64p]),
+    "nb_engine_sync": (ctypes.c_int, [_h]),
     "nb_batch_poll": (ctypes.c_int, [_h, ctypes.c_int64, _i32p, _i64p]),
     "nb_batch_fetch": (ctypes.c_int, [_h, ctypes.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]),
     "nb_batch_cancel": (ctypes.c_int, [_h, ctypes.c_int64]),

@@ -81,6 +81,18 @@ class Engine:
         self._ck(self._lib.nb_engine_run(self.handle, int(max_steps), ctypes.byref(k)))
         return k.value
 
+    def run_async(self, max_steps=1 << 62):
+        """nb_engine_run_async: completes the chunk in flight (if any), admits,
+        launches the next chunk and returns while the GPU runs it; returns its
+        step count (0: nothing resident)."""
+        k = ctypes.c_int64()
+        self._ck(self._lib.nb_engine_run_async(self.handle, int(max_steps), ctypes.byref(k)))
+        return k.value
+
+    def sync(self):
+        """Waits for the chunk left by run_async."""
+        self._ck(self._lib.nb_engine_sync(self.handle))
+
     def run_until_idle(self):
         while True:
             st = self.stats()

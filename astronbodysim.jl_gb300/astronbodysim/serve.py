@@ -57,15 +57,36 @@ class RequestStream:
         return {"pos": pos, "vel": vel, "mass": np.full(req["n"], 1.0 / req["n"])}
 
 
+def _percentiles(x):
+    x = np.asarray(x, dtype=float)
+    if not x.size:
+        return {"n": 0, "p50_s": None, "p99_s": None}
+    return {"n": int(x.size), "p50_s": float(np.percentile(x, 50)),
+            "p99_s": float(np.percentile(x, 99))}
+
+
 def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_after=False,
-          log=None, policy="fifo"):
+          log=None, policy="fifo", overlap=True):
     """Run the request loop for `duration` seconds of wall time.  Arrivals stop
     at `duration`; with drain_after the loop then continues until every arrived
     request has finished.  policy "fifo" hands requests to the engine in
     arrival order; "sjf" hands the waiting request with the least work
-    (N^2 x steps) first.  Returns latency / throughput statistics."""
+    (N^2 x steps) first.
+
+    With overlap (and an engine that has run_async) each chunk of engine steps
+    is only launched; while the GPU runs it the loop takes new arrivals,
+    builds their initial conditions, submits them and collects finished
+    results, and the engine admits the submitted systems at the next chunk
+    boundary.  Without it every chunk is run to completion first.
+
+    Latency = completion time - arrival time.  Two sets of percentiles are
+    reported: over the completed requests only, and over every offered
+    request, where a request still waiting or running at the end counts with
+    its age at the end -- a lower bound of its latency (right-censored), so
+    under overload these figures are lower bounds, not estimates."""
     if policy not in ("fifo", "sjf"):
         raise ValueError("policy must be 'fifo' or 'sjf'")
+    overlap = overlap and hasattr(engine, "run_async")
     t0 = time.perf_counter()
     pending = []          # arrived, not yet handed to the engine
     inflight = {}         # engine id -> request
@@ -75,6 +96,16 @@ def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_a
     offered_pairs = 0.0
     done_pairs = 0.0
     st0 = engine.stats()
+    running_chunk = False
+
+    def collect(tdone):
+        nonlocal done_pairs
+        for rid in engine.drain_done():
+            req = inflight.pop(rid)
+            lat.append(tdone - req["arrival"])
+            done_pairs += float(req["n"]) ** 2 * req["nsteps"]
+            engine.fetch(rid, req["n"])
+
     while True:
         now = time.perf_counter() - t0
         while nxt["arrival"] <= min(now, duration):
@@ -82,8 +113,7 @@ def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_a
             offered += 1
             offered_pairs += float(nxt["n"]) ** 2 * nxt["nsteps"]
             nxt = stream.next()
-        st = engine.stats()
-        queued = st["queued"]
+        queued = engine.stats()["queued"]
         if policy == "sjf" and len(pending) > 1:
             pending.sort(key=lambda r: float(r["n"]) ** 2 * r["nsteps"])
         while pending and queued < max_engine_queue:
@@ -92,22 +122,26 @@ def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_a
             inflight[rid] = req
             queued += 1
         if inflight:
-            engine.run(chunk_steps)
+            if overlap:
+                k = engine.run_async(chunk_steps)  # waits for the previous chunk, launches the next
+                running_chunk = k > 0
+            else:
+                engine.run(chunk_steps)
             tdone = time.perf_counter() - t0
-            for rid in engine.drain_done():
-                req = inflight.pop(rid)
-                lat.append(tdone - req["arrival"])
-                done_pairs += float(req["n"]) ** 2 * req["nsteps"]
-                engine.fetch(rid, req["n"])
+            collect(tdone)
             if log:
                 log(len(lat), tdone)
         elif now < duration:
             time.sleep(max(0.0, min(nxt["arrival"], duration) - now))
         if now >= duration and (not drain_after or (not pending and not inflight)):
             break
+    if running_chunk:
+        engine.sync()
+        collect(time.perf_counter() - t0)
     wall = time.perf_counter() - t0
     st1 = engine.stats()
     lat = np.array(lat)
+    censored = [wall - r["arrival"] for r in pending] + [wall - r["arrival"] for r in inflight.values()]
     served = st1["interactions"] - st0["interactions"]
     gpu_s = (st1["gpu_ms"] - st0["gpu_ms"]) / 1e3
     return {
@@ -117,8 +151,9 @@ def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_a
         "offered_rate_per_s": offered / duration,
         "offered_interactions_per_s": offered_pairs / duration,
         "completed": int(lat.size),
-        "latency_p50_s": float(np.percentile(lat, 50)) if lat.size else None,
-        "latency_p99_s": float(np.percentile(lat, 99)) if lat.size else None,
+        "latency_completed": _percentiles(lat),
+        "latency_all_requests_lower_bound": dict(_percentiles(np.concatenate([lat, censored])),
+                                                 censored=len(censored)),
         "served_interactions": served,
         "served_interactions_per_s_wall": served / wall,
         "served_interactions_per_s_gpu": served / gpu_s if gpu_s > 0 else None,
@@ -126,6 +161,7 @@ def serve(engine, stream, duration, chunk_steps=16, max_engine_queue=32, drain_a
         "backlog_requests": len(pending) + len(inflight),
         "resident_at_end": st1["running"],
         "policy": policy,
+        "overlap": overlap,
     }
 
 

@@ -106,6 +106,8 @@ struct nb_engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     nb_engine_stats stats{};
     std::vector<int64_t> finished;  // ids retired since the last nb_engine_drain_done
+    bool inflight = false;           // a chunk of steps launched by nb_engine_run_async
+    int64_t inflight_k = 0;          // its step count
 };
 
 namespace {
@@ -436,6 +438,83 @@ int retire(nb_engine* e) {
     return NB_OK;
 }
 
+// Admission and start-up before a chunk of steps: retire finished systems,
+// admit queued ones, rebuild the rank tables, start the admitted systems.
+int prepare_chunk(nb_engine* e) {
+    int rc = retire(e);  // systems submitted with nsteps == 0 or finished earlier
+    if (rc) return rc;
+    std::vector<int32_t> admitted;
+    rc = admit(e, admitted);
+    if (rc) return rc;
+    if (e->dirty) {
+        rc = rebuild(e);
+        if (rc) return rc;
+    }
+    return start_systems(e, admitted);
+}
+
+// Launch up to max_steps engine steps (fewer when a system finishes earlier or
+// max_steps_per_call is reached) as graph replays between two events; *k is
+// the step count (0: nothing to run).  No synchronisation.
+int launch_chunk(nb_engine* e, int64_t max_steps, int64_t* k_out) {
+    *k_out = 0;
+    if (e->nrank == 0) return NB_OK;
+    int64_t k = std::min<int64_t>(max_steps, e->p.max_steps_per_call);
+    for (int32_t s = 0; s < (int32_t)e->slot_req.size(); ++s) {
+        if (e->slot_req[s] < 0) continue;
+        const Request& q = e->reqs[e->slot_req[s]];
+        if (q.state == NB_REQ_RUNNING) k = std::min<int64_t>(k, q.nsteps - q.steps_done);
+    }
+    if (k <= 0) return NB_OK;
+    if (!e->graph) {
+        cudaGraph_t g = nullptr;
+        NE_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t r1 = enqueue_step(e, e->stream);
+        cudaError_t r2 = cudaStreamEndCapture(e->stream, &g);
+        if (r1 != cudaSuccess || r2 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return efail(e, NB_ERR_CUDA, "engine step capture failed: %s",
+                         cudaGetErrorString(r1 != cudaSuccess ? r1 : r2));
+        }
+        cudaError_t r3 = cudaGraphInstantiate(&e->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (r3 != cudaSuccess) {
+            e->graph = nullptr;
+            return efail(e, NB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(r3));
+        }
+    }
+    NE_CK(cudaEventRecord(e->ev0, e->stream));
+    for (int64_t i = 0; i < k; ++i) NE_CK(cudaGraphLaunch(e->graph, e->stream));
+    NE_CK(cudaEventRecord(e->ev1, e->stream));
+    *k_out = k;
+    return NB_OK;
+}
+
+// Wait for a launched chunk of k steps, account it and retire the systems it
+// finished.
+int complete_chunk(nb_engine* e, int64_t k) {
+    int rc = check_err(e);
+    if (rc) return rc;
+    float ms = 0.0f;
+    NE_CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    e->stats.gpu_ms += ms;
+    e->stats.engine_steps += k;
+    e->stats.interactions += (double)k * e->pairs_per_step;
+    for (int32_t s = 0; s < (int32_t)e->slot_req.size(); ++s) {
+        if (e->slot_req[s] < 0) continue;
+        Request& q = e->reqs[e->slot_req[s]];
+        if (q.state == NB_REQ_RUNNING) q.steps_done += k;
+    }
+    return retire(e);
+}
+
+// Completes the chunk an nb_engine_run_async call left running, if any.
+int finish_inflight(nb_engine* e) {
+    if (!e->inflight) return NB_OK;
+    e->inflight = false;
+    return complete_chunk(e, e->inflight_k);
+}
+
 }  // namespace
 
 extern "C" {
@@ -537,6 +616,7 @@ int nb_engine_destroy(nb_engine* e) {
     if (!e) return NB_ERR_INVALID_ARG;
     cudaSetDevice(e->dev);
     cudaStreamSynchronize(e->stream);
+    e->inflight = false;
     drop_graph(e);
     if (e->ev0) cudaEventDestroy(e->ev0);
     if (e->ev1) cudaEventDestroy(e->ev1);
@@ -576,62 +656,47 @@ int nb_engine_run(nb_engine* e, int64_t max_steps, int64_t* steps_done) {
     if (!e || max_steps < 0) return NB_ERR_INVALID_ARG;
     if (steps_done) *steps_done = 0;
     NE_CK(cudaSetDevice(e->dev));
-    int rc = retire(e);  // systems submitted with nsteps == 0 or finished earlier
+    int rc = finish_inflight(e);
     if (rc) return rc;
-    std::vector<int32_t> admitted;
-    rc = admit(e, admitted);
+    rc = prepare_chunk(e);
     if (rc) return rc;
-    if (e->dirty) {
-        rc = rebuild(e);
-        if (rc) return rc;
-    }
-    rc = start_systems(e, admitted);
+    int64_t k = 0;
+    rc = launch_chunk(e, max_steps, &k);
     if (rc) return rc;
-    if (e->nrank == 0) return NB_OK;
-    int64_t k = std::min<int64_t>(max_steps, e->p.max_steps_per_call);
-    for (int32_t s = 0; s < (int32_t)e->slot_req.size(); ++s) {
-        if (e->slot_req[s] < 0) continue;
-        const Request& q = e->reqs[e->slot_req[s]];
-        if (q.state == NB_REQ_RUNNING) k = std::min<int64_t>(k, q.nsteps - q.steps_done);
-    }
     if (k > 0) {
-        if (!e->graph) {
-            cudaGraph_t g = nullptr;
-            NE_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-            cudaError_t r1 = enqueue_step(e, e->stream);
-            cudaError_t r2 = cudaStreamEndCapture(e->stream, &g);
-            if (r1 != cudaSuccess || r2 != cudaSuccess) {
-                if (g) cudaGraphDestroy(g);
-                return efail(e, NB_ERR_CUDA, "engine step capture failed: %s",
-                             cudaGetErrorString(r1 != cudaSuccess ? r1 : r2));
-            }
-            cudaError_t r3 = cudaGraphInstantiate(&e->graph, g, 0);
-            cudaGraphDestroy(g);
-            if (r3 != cudaSuccess) {
-                e->graph = nullptr;
-                return efail(e, NB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(r3));
-            }
-        }
-        NE_CK(cudaEventRecord(e->ev0, e->stream));
-        for (int64_t i = 0; i < k; ++i) NE_CK(cudaGraphLaunch(e->graph, e->stream));
-        NE_CK(cudaEventRecord(e->ev1, e->stream));
-        rc = check_err(e);
+        rc = complete_chunk(e, k);
         if (rc) return rc;
-        float ms = 0.0f;
-        NE_CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
-        e->stats.gpu_ms += ms;
-        e->stats.engine_steps += k;
-        e->stats.interactions += (double)k * e->pairs_per_step;
-        for (int32_t s = 0; s < (int32_t)e->slot_req.size(); ++s) {
-            if (e->slot_req[s] < 0) continue;
-            Request& q = e->reqs[e->slot_req[s]];
-            if (q.state == NB_REQ_RUNNING) q.steps_done += k;
-        }
+    } else {
+        rc = retire(e);
+        if (rc) return rc;
     }
-    rc = retire(e);
-    if (rc) return rc;
     if (steps_done) *steps_done = k;
     return NB_OK;
+}
+
+int nb_engine_run_async(nb_engine* e, int64_t max_steps, int64_t* steps_launched) {
+    if (!e || max_steps < 0) return NB_ERR_INVALID_ARG;
+    if (steps_launched) *steps_launched = 0;
+    NE_CK(cudaSetDevice(e->dev));
+    int rc = finish_inflight(e);
+    if (rc) return rc;
+    rc = prepare_chunk(e);
+    if (rc) return rc;
+    int64_t k = 0;
+    rc = launch_chunk(e, max_steps, &k);
+    if (rc) return rc;
+    if (k > 0) {
+        e->inflight = true;
+        e->inflight_k = k;
+    }
+    if (steps_launched) *steps_launched = k;
+    return NB_OK;
+}
+
+int nb_engine_sync(nb_engine* e) {
+    if (!e) return NB_ERR_INVALID_ARG;
+    NE_CK(cudaSetDevice(e->dev));
+    return finish_inflight(e);
 }
 
 int nb_batch_poll(nb_engine* e, int64_t id, int32_t* state, int64_t* steps_done) {
@@ -659,6 +724,11 @@ int nb_batch_fetch(nb_engine* e, int64_t id, double* x, double* y, double* z, do
 
 int nb_batch_cancel(nb_engine* e, int64_t id) {
     if (!e) return NB_ERR_INVALID_ARG;
+    if (e->inflight) {
+        NE_CK(cudaSetDevice(e->dev));
+        int rc = finish_inflight(e);
+        if (rc) return rc;
+    }
     auto it = e->reqs.find(id);
     if (it == e->reqs.end()) return efail(e, NB_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
     Request& q = it->second;
@@ -678,6 +748,11 @@ int nb_batch_cancel(nb_engine* e, int64_t id) {
 
 int nb_batch_suspend(nb_engine* e, int64_t id) {
     if (!e) return NB_ERR_INVALID_ARG;
+    if (e->inflight) {
+        NE_CK(cudaSetDevice(e->dev));
+        int rc = finish_inflight(e);
+        if (rc) return rc;
+    }
     auto it = e->reqs.find(id);
     if (it == e->reqs.end()) return efail(e, NB_ERR_NOT_FOUND, "unknown request %lld", (long long)id);
     Request& q = it->second;

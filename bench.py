@@ -475,12 +475,22 @@ def run_gpu(args):
     # ---- serving sample (Poisson arrivals, continuous batching) ------------
     serve_stats = None
     if args.serve_seconds > 0:
-        stream = nb.RequestStream(rate=args.serve_rate, seed=7 + rank)
-        eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
-                        max_steps_per_call=args.serve_chunk, device=local, law=args.law)
-        serve_stats = nb.serve(eng, stream, args.serve_seconds, chunk_steps=args.serve_chunk)
-        eng.close()
-        serve_stats["arena_particles"] = args.serve_particles
+        serve_stats = {}
+        # the stated stream (overloaded on one GPU) and a sustainable load
+        # (offered ~0.8 of what one GB300 serves), drained to the last request
+        for name, rate, seconds, drain in (
+                ("lambda_%g" % args.serve_rate, args.serve_rate, args.serve_seconds, False),
+                ("lambda_%g_drained" % args.serve_sustainable_rate, args.serve_sustainable_rate,
+                 args.serve_sustainable_seconds, True)):
+            if seconds <= 0:
+                continue
+            stream = nb.RequestStream(rate=rate, seed=7 + rank)
+            eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
+                            max_steps_per_call=args.serve_chunk, device=local, law=args.law)
+            st = nb.serve(eng, stream, seconds, chunk_steps=args.serve_chunk, drain_after=drain)
+            eng.close()
+            st.update(rate=rate, arena_particles=args.serve_particles, chunk_steps=args.serve_chunk)
+            serve_stats[name] = st
 
     # ---- aggregate over ranks (replicas) -----------------------------------
     value, e2e_value, total_s, t_e2e = replica_rates(ws, args.steps, args.e2e_steps, n,
@@ -710,17 +720,21 @@ def run_serve(args):
     """Serving run alone (Poisson stream, continuous batching) -- one JSON line."""
     import astronbodysim as nb
 
-    stream = nb.RequestStream(rate=args.serve_rate, seed=7)
-    eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
-                    max_steps_per_call=args.serve_chunk, law=args.law)
-    st = nb.serve(eng, stream, args.serve_seconds, chunk_steps=args.serve_chunk,
-                  policy=args.serve_policy, max_engine_queue=args.serve_queue,
-                  log=lambda k, t: print("completed %d at %.1f s" % (k, t), file=sys.stderr)
-                  if k and k % 100 == 0 else None)
-    eng.close()
-    st.update({"mode": "serve", "rate": args.serve_rate, "arena_particles": args.serve_particles,
-               "chunk_steps": args.serve_chunk, "unit": UNIT})
-    print(json.dumps(st), flush=True)
+    out = {"mode": "serve", "rate": args.serve_rate, "arena_particles": args.serve_particles,
+           "chunk_steps": args.serve_chunk, "unit": UNIT, "seconds": args.serve_seconds,
+           "drain_after": args.serve_drain}
+    policies = ["fifo", "sjf"] if args.serve_policy == "both" else [args.serve_policy]
+    for pol in policies:
+        stream = nb.RequestStream(rate=args.serve_rate, seed=7)  # the same arrivals for each policy
+        eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
+                        max_steps_per_call=args.serve_chunk, law=args.law)
+        st = nb.serve(eng, stream, args.serve_seconds, chunk_steps=args.serve_chunk,
+                      policy=pol, max_engine_queue=args.serve_queue, drain_after=args.serve_drain,
+                      log=lambda k, t: print("completed %d at %.1f s" % (k, t), file=sys.stderr)
+                      if k and k % 100 == 0 else None)
+        eng.close()
+        out[pol] = st
+    print(json.dumps(out), flush=True)
     return 0
 
 
@@ -752,7 +766,10 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=200.0)
     ap.add_argument("--serve-chunk", type=int, default=16)
     ap.add_argument("--serve-particles", type=int, default=1 << 22)
-    ap.add_argument("--serve-policy", default="fifo", choices=["fifo", "sjf"])
+    ap.add_argument("--serve-policy", default="fifo", choices=["fifo", "sjf", "both"])
+    ap.add_argument("--serve-drain", action="store_true")
+    ap.add_argument("--serve-sustainable-rate", type=float, default=2.0)
+    ap.add_argument("--serve-sustainable-seconds", type=float, default=30.0)
     ap.add_argument("--serve-queue", type=int, default=32)
     ap.add_argument("--mode", default="bench", choices=["bench", "serve", "collision", "tune", "ensemble",
                                                          "plummer4096"])

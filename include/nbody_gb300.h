@@ -346,6 +346,16 @@ int nb_batch_submit(nb_engine *e, int64_t n, const double *x, const double *y, c
  * (fewer when a system finishes earlier or max_steps_per_call is reached);
  * finished systems are retired and their results kept for nb_batch_fetch. */
 int nb_engine_run(nb_engine *e, int64_t max_steps, int64_t *steps_done);
+/* The same as nb_engine_run, but the chunk of steps is only launched: the
+ * call returns while the GPU works, so the caller can build and submit new
+ * requests meanwhile (submit, poll, fetch and drain_done are host-side and do
+ * not wait).  The next nb_engine_run / nb_engine_run_async / nb_engine_sync
+ * (and cancel or suspend) first waits for the chunk, accounts it and retires
+ * the systems it finished.  *steps_launched = steps of the chunk (0: nothing
+ * was resident).  Statistics lag by the chunk in flight. */
+int nb_engine_run_async(nb_engine *e, int64_t max_steps, int64_t *steps_launched);
+/* Waits for the chunk left by nb_engine_run_async, if any. */
+int nb_engine_sync(nb_engine *e);
 int nb_batch_poll(nb_engine *e, int64_t id, int32_t *state, int64_t *steps_done);
 /* Copy the final positions and velocities of a finished system (then forget it). */
 int nb_batch_fetch(nb_engine *e, int64_t id, double *x, double *y, double *z, double *vx,

@@ -187,3 +187,41 @@ def test_engine_launch_shapes_agree(nb, shape):
 def test_engine_rejects_unknown_shape(nb):
     with pytest.raises(nb.NbodyError):
         nb.Engine(max_particles=1 << 12, max_systems=4, block=512, i_per_thread=1)
+
+
+def test_run_async_matches_blocking_run(nb):
+    """Chunks launched with run_async (completed by the next call) and systems
+    submitted while a chunk runs give results bit-identical to the same
+    systems run with the blocking run()."""
+    sizes = [400, 1500, 260, 3000, 900]
+    softs = [0.01, 0.004, 0.02, 0.003, 0.008]
+    steps = [30, 17, 45, 22, 9]
+    ds = systems(nb, sizes, seed=21)
+    out = {}
+    for mode in ("blocking", "async"):
+        eng = nb.Engine(max_particles=1 << 15, max_systems=16, max_steps_per_call=8)
+        ids = {}
+        if mode == "blocking":
+            for k in range(5):
+                ids[k] = eng.submit(ds[k], softs[k], 1e-3, steps[k])
+            eng.run_until_idle()
+        else:
+            for k in range(2):
+                ids[k] = eng.submit(ds[k], softs[k], 1e-3, steps[k])
+            launched = eng.run_async(8)
+            assert launched == 8
+            # submitted while the first chunk runs; admitted at the next boundary
+            for k in range(2, 5):
+                ids[k] = eng.submit(ds[k], softs[k], 1e-3, steps[k])
+            while True:
+                st = eng.stats()
+                if eng.run_async(8) == 0 and st["queued"] == 0:
+                    break
+            eng.sync()
+        for k in range(5):
+            assert eng.poll(ids[k])[0] == nb._lib.NB_REQ_DONE, (mode, k)
+            out[(mode, k)] = eng.fetch(ids[k], sizes[k])
+        eng.close()
+    for k in range(5):
+        np.testing.assert_array_equal(out[("async", k)]["pos"], out[("blocking", k)]["pos"])
+        np.testing.assert_array_equal(out[("async", k)]["vel"], out[("blocking", k)]["vel"])

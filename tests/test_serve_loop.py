@@ -55,9 +55,67 @@ def test_serve_accounts_every_request(policy):
     st = serve(eng, stream, 0.05, drain_after=True, policy=policy, max_engine_queue=1)
     assert st["completed"] == st["offered_requests"] > 0
     assert st["backlog_requests"] == 0
-    assert st["latency_p50_s"] <= st["latency_p99_s"]
-    assert st["policy"] == policy
+    lc, la = st["latency_completed"], st["latency_all_requests_lower_bound"]
+    assert lc["p50_s"] <= lc["p99_s"]
+    # drained: every offered request completed, nothing censored
+    assert la["n"] == lc["n"] == st["offered_requests"] and la["censored"] == 0
+    assert la["p99_s"] == lc["p99_s"]
+    assert st["policy"] == policy and not st["overlap"]
     assert st["served_interactions"] == pytest.approx(st["completed_interactions"])
+
+
+def test_overload_counts_unfinished_requests_as_censored():
+    """Under overload the completed-only percentiles see only the lucky
+    requests; the all-requests figures count every unfinished request with
+    its age at the end (a lower bound of its latency)."""
+    stream = RequestStream(rate=3000.0, seed=5, n_min=128, n_max=256, steps_min=40000, steps_max=50000,
+                           pool_size=1)
+    eng = FakeEngine()
+    st = serve(eng, stream, 0.05, policy="fifo", max_engine_queue=4)
+    la = st["latency_all_requests_lower_bound"]
+    assert st["backlog_requests"] > 0 and la["censored"] == st["backlog_requests"]
+    assert la["n"] == st["offered_requests"] == st["completed"] + la["censored"]
+    if st["completed"]:
+        assert la["p50_s"] >= 0.0
+
+
+class FakeAsyncEngine(FakeEngine):
+    """run_async launches a chunk that completes at the next run_async or
+    sync call, as nb_engine_run_async does; records whether submits happened
+    while a chunk was in flight."""
+
+    def __init__(self):
+        super().__init__()
+        self.pending_chunk = False
+        self.submits_in_flight = 0
+
+    def submit(self, data, eps, dt, nsteps):
+        if self.pending_chunk:
+            self.submits_in_flight += 1
+        return super().submit(data, eps, dt, nsteps)
+
+    def run_async(self, max_steps=16):
+        self.sync()
+        if self.running is None and not self.queue:
+            return 0
+        self.pending_chunk = True
+        return max_steps
+
+    def sync(self):
+        if self.pending_chunk:
+            self.pending_chunk = False
+            FakeEngine.run(self)
+
+
+def test_overlapped_loop_submits_while_a_chunk_runs():
+    stream = RequestStream(rate=2000.0, seed=6, n_min=64, n_max=128, steps_min=10, steps_max=20,
+                           pool_size=1)
+    eng = FakeAsyncEngine()
+    st = serve(eng, stream, 0.05, drain_after=True, max_engine_queue=64)
+    assert st["overlap"]
+    assert st["completed"] == st["offered_requests"] > 0 and st["backlog_requests"] == 0
+    assert eng.submits_in_flight > 0
+    assert not eng.pending_chunk
 
 
 def test_sjf_hands_over_the_smallest_waiting_request_first():
