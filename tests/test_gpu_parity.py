@@ -353,10 +353,11 @@ def test_builtin_rule_at_large_n_matches_explicit_shape_and_oracle(nb, oracle):
     nb.compute_force(a)
     np.testing.assert_array_equal(ga, nb.get_all_data(a)["acc"])
     nb.compute_force(b)
-    # two mixed forms (two targets per thread with the j-split against one
-    # target per thread unsplit) differ by their own FP32 round-off
+    # two mixed forms (tiles of 512, two targets per thread and the j-split
+    # against tiles of 256, one target per thread unsplit) differ by their own
+    # FP32 round-off: the mixed-form bars
     er = rel_err(ga, nb.get_all_data(b)["acc"])
-    assert np.median(er) <= 1e-7 and er.max() <= 1e-5
+    assert np.median(er) <= 1e-6 and np.quantile(er, 0.99) <= 1e-5 and er.max() <= 1e-4
     sub = np.arange(0, n, 512)
     a_ref, _ = oracle.force(d["pos"], d["mass"], d["pos"][sub], h)
     e = rel_err(ga[sub], a_ref)
