@@ -716,6 +716,22 @@ def run_collision(args):
     return 0
 
 
+def run_fp64(args):
+    """The plain FP64 form alone: acceleration at --fp64-targets seeded
+    particles of the Plummer sphere of --n from all its particles (one
+    k_force_fp64 launch, CUDA events) -- one JSON line."""
+    import torch
+
+    import astronbodysim as nb
+
+    data = nb.plummer(args.n, seed=2)
+    stream = torch.cuda.Stream()
+    out = fp64_leg(nb, data, args, 0, stream, args.fp64_targets)
+    out.update(mode="fp64", n=args.n, law=args.law)
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_serve(args):
     """Serving run alone (Poisson stream, continuous batching) -- one JSON line."""
     import astronbodysim as nb
@@ -771,7 +787,7 @@ def main():
     ap.add_argument("--serve-sustainable-rate", type=float, default=2.0)
     ap.add_argument("--serve-sustainable-seconds", type=float, default=30.0)
     ap.add_argument("--serve-queue", type=int, default=32)
-    ap.add_argument("--mode", default="bench", choices=["bench", "serve", "collision", "tune", "ensemble",
+    ap.add_argument("--mode", default="bench", choices=["bench", "serve", "collision", "tune", "ensemble", "fp64",
                                                          "plummer4096"])
     ap.add_argument("--n-each", type=int, default=1 << 20)
     ap.add_argument("--base-steps", type=int, default=2)
@@ -791,6 +807,8 @@ def main():
         return run_reference(args)
     if args.mode == "serve":
         return run_serve(args)
+    if args.mode == "fp64":
+        return run_fp64(args)
     if args.mode == "collision":
         return run_collision(args)
     if args.mode == "plummer4096":
