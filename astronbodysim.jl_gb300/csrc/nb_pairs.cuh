@@ -276,14 +276,16 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
                                                        const float* hh, const float* h2, float* ax,
                                                        float* ay, float* az, float* ap, float mu) {
     // Two passes over the tile.  Pass 1 is the packed FP32x2 loop of
-    // pair_loop_fast (uniform-mass form and split sums included) with the
-    // Newtonian factor of every r < h half set to zero by a select (so the
-    // self pair, r = 0, adds nothing); a 16-bit mask records which blocks of 8
-    // source pairs held such a half.  Pass 2 revisits only the blocks that
-    // some lane of the warp flagged and adds the spline terms of their r < h
-    // pairs.
+    // pair_loop_fast (uniform-mass form and split sums included) on r^2
+    // clamped to at least h^2: a pair with r < h adds the bounded Newtonian
+    // term of distance h, m d / h^3 (the self pair, d = 0, adds no force),
+    // and the smallest unclamped r^2 of every block of 8 source pairs marks
+    // the blocks that held such a pair.  Pass 2 revisits only the blocks that
+    // some lane of the warp flagged and replaces, for each r < h pair, the
+    // clamped term by the spline term.  Both terms are at most about m / h^2,
+    // so the replacement loses nothing to cancellation.
     constexpr int NA = LoopShape<IPT>::NA;
-    float2 nx[IPT], ny[IPT], nz[IPT];
+    float2 nx[IPT], ny[IPT], nz[IPT], hc[IPT];
     float2 sx[NA][IPT], sy[NA][IPT], sz[NA][IPT], sp[NA][IPT];
     uint32_t blk = 0;  // bit q: a r < h half among source pairs 8q .. 8q + 7
 #pragma unroll
@@ -291,42 +293,48 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
         nx[k] = make_float2(-xr[k], -xr[k]);
         ny[k] = make_float2(-yr[k], -yr[k]);
         nz[k] = make_float2(-zr[k], -zr[k]);
+        hc[k] = make_float2(h2[k], h2[k]);
 #pragma unroll
         for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
-#pragma unroll (LoopShape<IPT>::UNROLL)
-    for (int p = 0; p < TJ / 2; p += NA) {
+#pragma unroll 1
+    for (int q = 0; q < TJ / 16; ++q) {
+        float rmin[IPT];
 #pragma unroll
-        for (int u = 0; u < NA; ++u) {
-            const float4 A = b[2 * (p + u)];
-            const float4 B = b[2 * (p + u) + 1];
-            const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
-            const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
+        for (int k = 0; k < IPT; ++k) rmin[k] = 3e38f;
 #pragma unroll
-            for (int k = 0; k < IPT; ++k) {
-                const float2 dx = __fadd2_rn(qx, nx[k]);
-                const float2 dy = __fadd2_rn(qy, ny[k]);
-                const float2 dz = __fadd2_rn(qz, nz[k]);
-                const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
-                const float2 rinv = make_float2(rsqrt_approx(r2.x), rsqrt_approx(r2.y));
-                float2 mp = UNI ? rinv : __fmul2_rn(qm, rinv);
-                float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
-                const bool cx = r2.x < h2[k], cy = r2.y < h2[k];
-                blk |= (uint32_t)(cx | cy) << ((p + u) >> 3);
-                mr3.x = cx ? 0.0f : mr3.x;
-                mr3.y = cy ? 0.0f : mr3.y;
-                if (ACC) {
-                    sx[u][k] = __ffma2_rn(dx, mr3, sx[u][k]);
-                    sy[u][k] = __ffma2_rn(dy, mr3, sy[u][k]);
-                    sz[u][k] = __ffma2_rn(dz, mr3, sz[u][k]);
-                }
-                if (POT) {
-                    mp.x = cx ? 0.0f : mp.x;
-                    mp.y = cy ? 0.0f : mp.y;
-                    sp[u][k] = __fadd2_rn(sp[u][k], mp);
+        for (int i = 0; i < 8; i += NA) {
+#pragma unroll
+            for (int u = 0; u < NA; ++u) {
+                const int p = 8 * q + i + u;
+                const float4 A = b[2 * p];
+                const float4 B = b[2 * p + 1];
+                const float2 qx = make_float2(A.x, A.y), qy = make_float2(A.z, A.w);
+                const float2 qz = make_float2(B.x, B.y), qm = make_float2(B.z, B.w);
+#pragma unroll
+                for (int k = 0; k < IPT; ++k) {
+                    const float2 dx = __fadd2_rn(qx, nx[k]);
+                    const float2 dy = __fadd2_rn(qy, ny[k]);
+                    const float2 dz = __fadd2_rn(qz, nz[k]);
+                    const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
+                    rmin[k] = fminf(rmin[k], fminf(r2.x, r2.y));
+                    const float2 rc = make_float2(fmaxf(r2.x, hc[k].x), fmaxf(r2.y, hc[k].y));
+                    const float2 rinv = make_float2(rsqrt_approx(rc.x), rsqrt_approx(rc.y));
+                    const float2 mp = UNI ? rinv : __fmul2_rn(qm, rinv);
+                    if (ACC) {
+                        const float2 mr3 = __fmul2_rn(__fmul2_rn(mp, rinv), rinv);
+                        sx[u][k] = __ffma2_rn(dx, mr3, sx[u][k]);
+                        sy[u][k] = __ffma2_rn(dy, mr3, sy[u][k]);
+                        sz[u][k] = __ffma2_rn(dz, mr3, sz[u][k]);
+                    }
+                    if (POT) sp[u][k] = __fadd2_rn(sp[u][k], mp);
                 }
             }
         }
+        bool f = false;
+#pragma unroll
+        for (int k = 0; k < IPT; ++k) f |= rmin[k] < h2[k];
+        blk |= (uint32_t)f << q;
     }
     // Fold the split sums (and the common mass) into one set.
     float2 tx[IPT], ty[IPT], tz[IPT], tp[IPT];
@@ -367,21 +375,29 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
                 const float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __fmul2_rn(dz, dz)));
                 const bool cx = r2.x < h2[k], cy = r2.y < h2[k];
                 if (__any_sync(0xffffffffu, cx | cy)) {
+                    // the clamped Newtonian term pass 1 added: m r_h^-3 d and m r_h^-1
+                    const float rh = rsqrt_approx(h2[k]);
                     if (cx) {
+                        const float m = UNI ? mu : qm.x;
                         float mr3, mp;
-                        spline_close(r2.x, rsqrt_approx(r2.x), UNI ? mu : qm.x, hh[k], mr3, mp);
-                        tx[k].x = fmaf(dx.x, mr3, tx[k].x);
-                        ty[k].x = fmaf(dy.x, mr3, ty[k].x);
-                        tz[k].x = fmaf(dz.x, mr3, tz[k].x);
-                        tp[k].x += mp;
+                        spline_close(r2.x, rsqrt_approx(r2.x), m, hh[k], mr3, mp);
+                        const float mrh = m * rh;
+                        const float d3 = mr3 - (mrh * rh) * rh;
+                        tx[k].x = fmaf(dx.x, d3, tx[k].x);
+                        ty[k].x = fmaf(dy.x, d3, ty[k].x);
+                        tz[k].x = fmaf(dz.x, d3, tz[k].x);
+                        tp[k].x += mp - mrh;
                     }
                     if (cy) {
+                        const float m = UNI ? mu : qm.y;
                         float mr3, mp;
-                        spline_close(r2.y, rsqrt_approx(r2.y), UNI ? mu : qm.y, hh[k], mr3, mp);
-                        tx[k].y = fmaf(dx.y, mr3, tx[k].y);
-                        ty[k].y = fmaf(dy.y, mr3, ty[k].y);
-                        tz[k].y = fmaf(dz.y, mr3, tz[k].y);
-                        tp[k].y += mp;
+                        spline_close(r2.y, rsqrt_approx(r2.y), m, hh[k], mr3, mp);
+                        const float mrh = m * rh;
+                        const float d3 = mr3 - (mrh * rh) * rh;
+                        tx[k].y = fmaf(dx.y, d3, tx[k].y);
+                        ty[k].y = fmaf(dy.y, d3, ty[k].y);
+                        tz[k].y = fmaf(dz.y, d3, tz[k].y);
+                        tp[k].y += mp - mrh;
                     }
                 }
             }
