@@ -75,7 +75,7 @@ class nb_params(ctypes.Structure):
         ("mond_acc0", ctypes.c_double),
         ("mond_nu_index", ctypes.c_double),
         ("stages", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("resort_every", ctypes.c_int32),
     ]
 
 

@@ -100,7 +100,7 @@ class Simulation:
                  TimeEnd=0.1, TimeBase=1 << 30, ErrTolTimestep=0.025, MinStep=1.0e-8,
                  MaxStep=float("inf"), law="spline", precision="mixed", criterion="ref",
                  device=None, block=0, i_per_thread=0, j_split=0, tile_j=0, stages=0, tuning=None,
-                 bgforce=None,
+                 resort_every=0, bgforce=None,
                  GravityModel=None, ACC0=0.0, MOND_nuIndex=2.0, TimeIntegrationAlgorithm=None,
                  TimeBetweenSnapshots=None, OutputFunc=None):
         self._lib = L.load()
@@ -153,6 +153,7 @@ class Simulation:
         p.j_split = int(j_split)
         p.tile_j = int(tile_j)
         p.stages = int(stages)
+        p.resort_every = int(resort_every)
         self.tuned_shape = (int(block), int(i_per_thread), int(j_split), int(tile_j), int(stages))
         self.params = p
         alg = TimeIntegrationAlgorithm
@@ -174,7 +175,8 @@ class Simulation:
         h = ctypes.c_void_p()
         rc = self._lib.nb_create(ctypes.byref(p), ctypes.byref(h))
         if rc != L.NB_OK:
-            raise L.NbodyError(rc, "nb_create failed (check parameters / device)")
+            why = self._lib.nb_last_error(None)
+            raise L.NbodyError(rc, "nb_create failed: %s" % (why.decode() if why else "?"))
         self.handle = h
         self.n = 0
         # sim.config.output.func: called with the simulation at every output
@@ -244,7 +246,8 @@ class Simulation:
                                               buf.size))
         p = L.nb_params.from_buffer_copy(image, _CKPT_PARAMS_OFFSET)
         n = int(np.frombuffer(image, dtype=np.int64, count=1, offset=16)[0])
-        arrays = 11 * 8 * n + (4 * n + 7) // 8 * 8 + 16 * n
+        # 11 FP64 arrays, types, two int64 bin arrays, the source permutation
+        arrays = 11 * 8 * n + 2 * ((4 * n + 7) // 8 * 8) + 16 * n
         hdr = len(image) - arrays
         self.params = p
         self.euler = p.algorithm == L.NB_ALG_EULER
@@ -347,7 +350,7 @@ def loadrestart(filename, device=None, OutputFunc=None):
                      precision=inv(PRECISIONS, p.precision), criterion=inv(CRITERIA, p.criterion),
                      device=p.device if device is None else device, block=p.block,
                      i_per_thread=p.i_per_thread, j_split=p.j_split, tile_j=p.tile_j,
-                     stages=p.stages,
+                     stages=p.stages, resort_every=p.resort_every,
                      TimeIntegrationAlgorithm=Euler if p.algorithm == L.NB_ALG_EULER else Leapfrog,
                      OutputFunc=OutputFunc)
     sim.restore(image)

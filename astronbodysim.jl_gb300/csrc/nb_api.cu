@@ -44,8 +44,16 @@ struct nb_handle {
     Clock* clk = nullptr;
     void* probe = nullptr;
     size_t probe_bytes = 0;
+    // Step graphs: [0] re-orders the sources (Morton sort) before the pack,
+    // [1] packs in the order of the last sort.  The host replays [0] every
+    // resort steps (and whenever the order is not valid) and [1] otherwise.
     cudaGraphExec_t step_exec = nullptr;
+    cudaGraphExec_t step_exec_nosort = nullptr;
     cudaGraphExec_t out_exec = nullptr;  // step graph that stops at output times
+    cudaGraphExec_t out_exec_nosort = nullptr;
+    int resort = 16;                      // steps between Morton sorts in the step graphs
+    bool perm_valid = false;              // perm holds an order of the current particles
+    int64_t host_steps = 0;               // steps completed by step graphs (device clock)
     double between = 0.0;                 // BetweenSnapshots (0: no output stops)
     int block = 128;
     int ipt = 2;
@@ -82,6 +90,9 @@ constexpr int64_t kAutoTile512From = 1 << 17;
 
 int auto_jsplit(int64_t n) { return n >= kAutoIpt2From ? 8 : 4; }
 int auto_tile(int64_t n) { return n >= kAutoTile512From ? 512 : 256; }
+
+// Reason the last nb_create on this thread failed (there is no handle to hold it).
+thread_local std::string g_create_err;
 
 int fail(nb_handle* h, int code, const char* fmt, ...) {
     if (h) {
@@ -176,12 +187,15 @@ int check_params(nb_handle* h, const nb_params* p) {
         return fail(h, NB_ERR_INVALID_ARG, "the work-list kernel takes tiles of %d sources", kTileJ);
     if (p->stages != 0 && p->stages != 3 && p->stages != 4 && p->stages != 6)
         return fail(h, NB_ERR_INVALID_ARG, "stages must be 0 (auto), 3, 4 or 6");
+    if (p->resort_every < 0 || p->resort_every > (1 << 20))
+        return fail(h, NB_ERR_INVALID_ARG, "resort_every must be 0 (auto) or 1..2^20");
     if (p->algorithm != NB_ALG_LEAPFROG && p->algorithm != NB_ALG_EULER)
         return fail(h, NB_ERR_INVALID_ARG, "algorithm must be NB_ALG_LEAPFROG or NB_ALG_EULER");
     return NB_OK;
 }
 
 void drop_graph(nb_handle* h) {
+    h->perm_valid = false;  // the next step graph replay sorts first
     if (h->step_exec) {
         cudaGraphExecDestroy(h->step_exec);
         h->step_exec = nullptr;
@@ -189,6 +203,14 @@ void drop_graph(nb_handle* h) {
     if (h->out_exec) {
         cudaGraphExecDestroy(h->out_exec);
         h->out_exec = nullptr;
+    }
+    if (h->step_exec_nosort) {
+        cudaGraphExecDestroy(h->step_exec_nosort);
+        h->step_exec_nosort = nullptr;
+    }
+    if (h->out_exec_nosort) {
+        cudaGraphExecDestroy(h->out_exec_nosort);
+        h->out_exec_nosort = nullptr;
     }
 }
 
@@ -229,7 +251,10 @@ nb::Targets particle_targets(nb_handle* h, bool want_acc, bool want_pot) {
 // Enqueue one force evaluation on stream s (no synchronisation).  With
 // active_only the targets are the particles with Ti_endstep == t_int
 // (src/directsum/gravity.jl:95-96); the list is built on the device.
-cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, bool active_only) {
+// sort = false packs the sources in the order of the last sort (perm must
+// hold a valid order; any order gives the same forces to FP32 round-off).
+cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, bool active_only,
+                          bool sort = true) {
     const bool pot = tg.pot != nullptr;
     const bool particles = tg.x == h->x;
     nb::Targets t2 = tg;
@@ -246,8 +271,10 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     }
     // Morton order of the sources keeps every j-tile compact, so the FP32
     // coordinates relative to its origin stay small.
-    e = nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, s);
-    if (e != cudaSuccess) return e;
+    if (sort) {
+        e = nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, s);
+        if (e != cudaSuccess) return e;
+    }
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, h->tj, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
     // Built-in choice (the size classes of kAutoIpt2From / kAutoTile512From
@@ -343,7 +370,7 @@ cudaError_t enqueue_post(nb_handle* h, cudaStream_t s, bool active_only) {
 }
 
 // Enqueue step(sim, DirectSum, GPU): drift -> force(active) -> kick.
-cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
+cudaError_t enqueue_step(nb_handle* h, cudaStream_t s, bool sort) {
     cudaError_t e;
     const bool adaptive = h->p.adaptive != 0;
     if (adaptive) {
@@ -357,7 +384,7 @@ cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
                              s);
         if (e != cudaSuccess) return e;
     }
-    e = enqueue_force(h, particle_targets(h, true, false), s, adaptive);
+    e = enqueue_force(h, particle_targets(h, true, false), s, adaptive, sort);
     if (e != cudaSuccess) return e;
     e = enqueue_post(h, s, adaptive);
     if (e != cudaSuccess) return e;
@@ -373,7 +400,7 @@ cudaError_t enqueue_step(nb_handle* h, cudaStream_t s) {
 // kernel sets the condition, so a replay either completes a step or stops the
 // time line at an output time inside it; the IF body is skipped on the device
 // without a host round trip.
-cudaError_t capture_output_graph(nb_handle* h, cudaGraphExec_t* out) {
+cudaError_t capture_output_graph(nb_handle* h, cudaGraphExec_t* out, bool sort) {
     *out = nullptr;
     cudaStream_t s = h->own_stream;
     const bool adaptive = h->p.adaptive != 0;
@@ -423,7 +450,7 @@ cudaError_t capture_output_graph(nb_handle* h, cudaGraphExec_t* out) {
         e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0,
                                           cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            e = enqueue_force(h, particle_targets(h, true, false), s, adaptive);
+            e = enqueue_force(h, particle_targets(h, true, false), s, adaptive, sort);
             if (e == cudaSuccess) e = enqueue_post(h, s, adaptive);
             if (e == cudaSuccess)
                 e = nb::launch_kick(h->vx, h->vy, h->vz, h->ax, h->ay, h->az, h->type, h->ti_beg,
@@ -537,6 +564,7 @@ void apply_tuning(nb_handle* h, const nb_params& p) {
     h->jsplit = p.j_split > 1 ? p.j_split : 1;
     h->tj = p.tile_j ? p.tile_j : kTileJ;
     h->stages = p.stages ? p.stages : 4;
+    h->resort = p.resort_every ? p.resort_every : 16;
     h->worklist = p.block == -1;
     h->auto_cfg = p.block == 0 && p.i_per_thread == 0;
 }
@@ -554,14 +582,19 @@ struct CkptHeader {
     int64_t clock_size;
     nb_params p;
     double between;  // BetweenSnapshots (0: no output stops)
-    double pad;
+    // Source order of the step graphs: the step count that sets the phase of
+    // their re-sorts, or -1 when the image holds no valid order (the
+    // permutation block after the bins then carries no meaning).
+    int64_t order_steps;
     Clock clk;
 };
 constexpr char kCkptMagic[8] = {'N', 'B', 'G', 'B', '3', '0', '0', 'C'};
-constexpr int64_t kCkptVersion = 2;
+constexpr int64_t kCkptVersion = 3;
 
+// Header, 11 FP64 arrays, types, two int64 bin arrays, the Morton permutation.
 int64_t ckpt_bytes(int64_t n) {
-    return (int64_t)sizeof(CkptHeader) + 11 * 8 * n + (int64_t)align_up(4 * (size_t)n, 8) + 16 * n;
+    return (int64_t)sizeof(CkptHeader) + 11 * 8 * n + 2 * (int64_t)align_up(4 * (size_t)n, 8) +
+           16 * n;
 }
 
 int require_particles(nb_handle* h) {
@@ -601,17 +634,24 @@ void nb_default_params(nb_params* p) {
 }
 
 int nb_create(const nb_params* p, nb_handle** out) {
-    if (!p || !out) return NB_ERR_INVALID_ARG;
+    g_create_err.clear();
+    if (!p || !out) {
+        g_create_err = "nb_create: null parameter or output pointer";
+        return NB_ERR_INVALID_ARG;
+    }
     *out = nullptr;
     nb_handle* h = new (std::nothrow) nb_handle();
     if (!h) return NB_ERR_OOM;
     int rc = check_params(h, p);
     if (rc) {
+        g_create_err = h->err;
         delete h;
         return rc;
     }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || p->device < 0 || p->device >= ndev) {
+        g_create_err = "nb_create: device " + std::to_string(p->device) + " not available (" +
+                       std::to_string(ndev) + " CUDA devices)";
         delete h;
         return NB_ERR_CUDA;
     }
@@ -704,15 +744,23 @@ int nb_upload(nb_handle* h, int64_t n, const double* x, const double* y, const d
                 return fail(h, NB_ERR_INVALID_ARG, "type[%lld]=%d outside 1..6", (long long)i, type[i]);
     int rc = use_device(h);
     if (rc) return rc;
+    const int64_t n_old = h->n;
+    const int tj_old = h->tj;
     if (n > 0) {
         if (h->auto_cfg && h->p.tile_j == 0) h->tj = auto_tile(n);
-        rc = ensure_capacity(h, n);
+        rc = ensure_capacity(h, n);  // drops the step graphs when it re-lays the arena out
         if (rc) return rc;
     }
     h->n = n;
     // tiles of this upload (the arena may hold more from a larger earlier one)
     h->ntiles = (int32_t)((n + h->tj - 1) / h->tj);
-    drop_graph(h);
+    // The step graphs hold the arena's pointers and the particle and tile
+    // counts, not the data: they stay valid for an upload of the same size.
+    // The source order of the old particles does not carry over.
+    if (n != n_old || h->tj != tj_old)
+        drop_graph(h);
+    else
+        h->perm_valid = false;
     if (n == 0) return NB_OK;
     const size_t d = sizeof(double) * (size_t)n;
     cudaStream_t s = h->stream;
@@ -983,13 +1031,24 @@ int nb_drift_to_float(nb_handle* h, double t_float) {
 // with stop_at_output the call returns at the first output time reached
 // (*at_output = 1), otherwise it continues through output times (the drift
 // is still split there).  *done = complete steps.
+// The step graphs that skip the sort read perm: give it an order of the
+// current particles first when none is known (after nb_create, nb_upload,
+// nb_checkpoint_load or a parameter change).
+static int ensure_order(nb_handle* h) {
+    if (h->perm_valid || h->p.precision == NB_PREC_FP64) return NB_OK;
+    NB_CK(nb::launch_morton_sort(h->x, h->y, h->z, h->n, h->sort_scratch, h->perm, h->stream));
+    h->perm_valid = true;
+    return NB_OK;
+}
+
 static int step_with_outputs(nb_handle* h, int64_t nsteps, bool stop_at_output, int64_t* done,
                       int32_t* at_output) {
     *done = 0;
     *at_output = 0;
-    if (!h->out_exec) {
+    if (!h->out_exec || !h->out_exec_nosort) {
         NB_CK(cudaStreamSynchronize(h->stream));
-        cudaError_t e = capture_output_graph(h, &h->out_exec);
+        cudaError_t e = capture_output_graph(h, &h->out_exec, true);
+        if (e == cudaSuccess) e = capture_output_graph(h, &h->out_exec_nosort, false);
         if (e != cudaSuccess)
             return fail(h, NB_ERR_CUDA, "output step graph capture failed: %s", cudaGetErrorString(e));
     }
@@ -1012,7 +1071,15 @@ static int step_with_outputs(nb_handle* h, int64_t nsteps, bool stop_at_output, 
         }
         int64_t chunk = nsteps - (st.steps - steps0);
         if (chunk > 32) chunk = 32;
-        for (int64_t k = 0; k < chunk; ++k) NB_CK(cudaGraphLaunch(h->out_exec, h->stream));
+        int rc0 = ensure_order(h);
+        if (rc0) return rc0;
+        for (int64_t k = 0; k < chunk; ++k) {
+            // Replay k performs step st.steps + k until one stops at an output
+            // time; the rest of the chunk is then skipped on the device and
+            // the next chunk starts from the device's count again.
+            const bool sort = (st.steps + k) % h->resort == 0;
+            NB_CK(cudaGraphLaunch(sort ? h->out_exec : h->out_exec_nosort, h->stream));
+        }
         int rc = sync_and_check(h);
         if (rc) return rc;
         NB_CK(cudaMemcpy(&c, h->clk, sizeof c, cudaMemcpyDeviceToHost));
@@ -1022,6 +1089,7 @@ static int step_with_outputs(nb_handle* h, int64_t nsteps, bool stop_at_output, 
     }
     *done = st.steps - steps0;
     *at_output = st.at_output;
+    h->host_steps = st.steps;
     return NB_OK;
 }
 
@@ -1037,27 +1105,37 @@ int nb_step(nb_handle* h, int64_t nsteps) {
         int32_t at = 0;
         return step_with_outputs(h, nsteps, false, &done, &at);
     }
-    if (!h->step_exec) {
-        // Capture one step on the handle's own (non-default) stream; the graph
-        // is then launched on whatever stream the handle currently uses.
-        cudaGraph_t g = nullptr;
+    if (!h->step_exec || !h->step_exec_nosort) {
+        // Capture one step (with and without the sort) on the handle's own
+        // (non-default) stream; the graphs are then launched on whatever
+        // stream the handle currently uses.
         NB_CK(cudaStreamSynchronize(h->stream));
-        NB_CK(cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t e = enqueue_step(h, h->own_stream);
-        cudaError_t e2 = cudaStreamEndCapture(h->own_stream, &g);
-        if (e != cudaSuccess || e2 != cudaSuccess) {
-            if (g) cudaGraphDestroy(g);
-            return fail(h, NB_ERR_CUDA, "step capture failed: %s",
-                        cudaGetErrorString(e != cudaSuccess ? e : e2));
-        }
-        e = cudaGraphInstantiate(&h->step_exec, g, 0);
-        cudaGraphDestroy(g);
-        if (e != cudaSuccess) {
-            h->step_exec = nullptr;
-            return fail(h, NB_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+        for (int variant = 0; variant < 2; ++variant) {
+            cudaGraph_t g = nullptr;
+            NB_CK(cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t e = enqueue_step(h, h->own_stream, variant == 0);
+            cudaError_t e2 = cudaStreamEndCapture(h->own_stream, &g);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return fail(h, NB_ERR_CUDA, "step capture failed: %s",
+                            cudaGetErrorString(e != cudaSuccess ? e : e2));
+            }
+            cudaGraphExec_t* dst = variant == 0 ? &h->step_exec : &h->step_exec_nosort;
+            e = cudaGraphInstantiate(dst, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                *dst = nullptr;
+                return fail(h, NB_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+            }
         }
     }
-    for (int64_t k = 0; k < nsteps; ++k) NB_CK(cudaGraphLaunch(h->step_exec, h->stream));
+    int rc0 = ensure_order(h);
+    if (rc0) return rc0;
+    for (int64_t k = 0; k < nsteps; ++k) {
+        const bool sort = h->host_steps % h->resort == 0;
+        NB_CK(cudaGraphLaunch(sort ? h->step_exec : h->step_exec_nosort, h->stream));
+        h->host_steps += 1;
+    }
     return sync_and_check(h);
 }
 
@@ -1224,6 +1302,7 @@ int nb_checkpoint_save(nb_handle* h, void* buf, int64_t bytes) {
     hd.clock_size = (int64_t)sizeof(Clock);
     hd.p = h->p;
     hd.between = h->between;
+    hd.order_steps = h->perm_valid ? h->host_steps : -1;
     NB_CK(cudaMemcpy(&hd.clk, h->clk, sizeof(Clock), cudaMemcpyDeviceToHost));
     char* b = static_cast<char*>(buf);
     std::memcpy(b, &hd, sizeof hd);
@@ -1240,6 +1319,11 @@ int nb_checkpoint_save(nb_handle* h, void* buf, int64_t bytes) {
         NB_CK(cudaMemcpyAsync(b + off, h->ti_beg, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
         off += sizeof(int64_t) * (size_t)n;
         NB_CK(cudaMemcpyAsync(b + off, h->ti_end, sizeof(int64_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        off += sizeof(int64_t) * (size_t)n;
+        if (h->perm_valid)
+            NB_CK(cudaMemcpyAsync(b + off, h->perm, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        else
+            std::memset(b + off, 0, align_up(4 * (size_t)n, 8));
         NB_CK(cudaStreamSynchronize(s));
     }
     return NB_OK;
@@ -1268,6 +1352,19 @@ int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
     for (int64_t i = 0; i < n; ++i)
         if (type[i] < 1 || type[i] > 6)
             return fail(h, NB_ERR_INVALID_ARG, "checkpoint type[%lld]=%d outside 1..6", (long long)i, type[i]);
+    // A saved source order is used only if it is a permutation of 0..n-1
+    // (the pack gathers through it); otherwise the next step re-sorts.
+    bool order_ok = hd.order_steps >= 0 && n > 0;
+    if (order_ok) {
+        const int32_t* pm = reinterpret_cast<const int32_t*>(
+            b + sizeof hd + 11 * 8 * (size_t)n + align_up(4 * (size_t)n, 8) + 16 * (size_t)n);
+        std::vector<unsigned char> seen((size_t)n, 0);
+        for (int64_t i = 0; i < n && order_ok; ++i) {
+            const int32_t v = pm[i];
+            if (v < 0 || v >= n || seen[(size_t)v]) order_ok = false;
+            else seen[(size_t)v] = 1;
+        }
+    }
     rc = use_device(h);
     if (rc) return rc;
     cudaStream_t s = h->stream;
@@ -1299,12 +1396,19 @@ int nb_checkpoint_load(nb_handle* h, const void* buf, int64_t bytes) {
     NB_CK(cudaMemcpyAsync(h->ti_beg, b + off, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, s));
     off += sizeof(int64_t) * (size_t)n;
     NB_CK(cudaMemcpyAsync(h->ti_end, b + off, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, s));
+    off += sizeof(int64_t) * (size_t)n;
+    if (order_ok) {
+        // the saved order lets the step graphs continue bit-identically
+        NB_CK(cudaMemcpyAsync(h->perm, b + off, sizeof(int32_t) * (size_t)n, cudaMemcpyHostToDevice, s));
+    }
     NB_CK(cudaStreamSynchronize(s));
+    h->perm_valid = order_ok;
+    h->host_steps = order_ok ? hd.order_steps : 0;
     return upload_sysdesc(h);
 }
 
 const char* nb_last_error(nb_handle* h) {
-    if (!h) return "null handle";
+    if (!h) return g_create_err.empty() ? "null handle" : g_create_err.c_str();
     return h->err.c_str();
 }
 

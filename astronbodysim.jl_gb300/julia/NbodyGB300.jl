@@ -63,7 +63,7 @@ struct NbParams
     mond_acc0::Float64
     mond_nu_index::Float64
     stages::Int32
-    reserved::Int32
+    resort_every::Int32
 end
 
 # Mirrors `nb_diag` of include/nbody_gb300.h.
@@ -159,7 +159,7 @@ function params(sim; precision = Int32(1), law = Int32(0), bgfield = nothing)
              bg_kind, mond, bg_gm, bg_center, bg_rg,
              mond == 0 ? 0.0 : strip(accunit(sim), sim.config.constants.ACC0),
              Float64(sim.config.grav.MOND_nuIndex),
-             Int32(0), Int32(0))       # stages (built-in), reserved
+             Int32(0), Int32(0))       # stages (built-in), resort_every (16)
 end
 
 """
@@ -184,7 +184,7 @@ function route(sim::Simulation; precision = :mixed, law = :spline, bgfield = not
                    law = Int32(law === :plummer ? 1 : 0), bgfield))
     out = Ref{Ptr{Cvoid}}(C_NULL)
     rc = ccall((:nb_create, libnb), Cint, (Ref{NbParams}, Ref{Ptr{Cvoid}}), p, out)
-    rc == 0 || error("nb_create failed: $rc")
+    check(C_NULL, rc)  # with a null handle nb_last_error gives the reason nb_create failed
     d = StructArray(Array(sim.simdata))
     dev = NbDeviceData(out[], length(d), d)
     finalizer(x -> ccall((:nb_destroy, libnb), Cint, (Ptr{Cvoid},), x.ptr), dev)

@@ -343,7 +343,8 @@ def run_gpu(args):
     sim = nb.Simulation(data, ForceSofteningTable=[EPS] * 6, TimeStep=DT, TimeEnd=1.0,
                         precision="mixed", law=args.law, device=local, block=args.block,
                         i_per_thread=args.ipt, j_split=args.jsplit, tile_j=args.tile, stages=args.stages,
-                        tuning=None if (args.block or args.ipt or args.jsplit) else "auto")
+                        tuning=None if (args.block or args.ipt or args.jsplit) else "auto",
+                        resort_every=1)
     tuned = sim.tuned_shape
     stream = torch.cuda.Stream(device=dev)
     sim.set_stream(stream.cuda_stream)
@@ -533,7 +534,8 @@ def run_gpu(args):
             "data": "synthetic (seeded Plummer sphere, G=M=a=1)",
             "config": {"workload": "plummer_n%d_eps1e-3_%s_mixed_kdk_dt1e-4" % (n, args.law),
                        "n": n, "law": args.law, "precision": "mixed (fp32 pairs, fp64 origins/state)",
-                       "step": "drift+pack+force(N^2)+kick, one CUDA graph replay",
+                       "step": "drift+Morton sort+pack+force(N^2)+kick, one CUDA graph replay "
+                               "(sort every step: resort_every=1)",
                        "l2": "256 MiB write between timed steps, outside the events",
                        "parallelism": "replicas" if ws > 1 else "single GPU",
                        "force_kernel": ("block=%d i_per_thread=%d j_split=%d tile=%d stages=%d (%s)" % (
@@ -694,6 +696,8 @@ def run_collision(args):
         nb.init_timesteps(sim)
         nb.leapfrog_half_kick(sim, +1)
         torch.cuda.synchronize()
+        sampler = ClockSampler(0)
+        sampler.start()
         t0 = time.perf_counter()
         while True:
             nb.step(sim, 1)
@@ -702,6 +706,7 @@ def run_collision(args):
                 break
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
+        clocks = sampler.stop()
         substeps, pairs = nb.counters(sim)
         nb.leapfrog_half_kick(sim, -1)
         d1 = nb.diagnostics(sim)
@@ -710,7 +715,8 @@ def run_collision(args):
                      "g_interactions_per_s": pairs / wall / 1e9,
                      "energy_rel_drift": (e1 - e0) / abs(e0),
                      "momentum_abs_drift": float(np.linalg.norm(d1["P"] - d0["P"])),
-                     "angular_momentum_abs_drift": float(np.linalg.norm(d1["L"] - d0["L"]))}
+                     "angular_momentum_abs_drift": float(np.linalg.norm(d1["L"] - d0["L"])),
+                     "clocks": clocks}
         sim.close()
     print(json.dumps(out), flush=True)
     return 0
@@ -741,6 +747,8 @@ def run_serve(args):
            "drain_after": args.serve_drain}
     policies = ["fifo", "sjf"] if args.serve_policy == "both" else [args.serve_policy]
     for pol in policies:
+        sampler = ClockSampler(0)
+        sampler.start()
         stream = nb.RequestStream(rate=args.serve_rate, seed=7)  # the same arrivals for each policy
         eng = nb.Engine(max_particles=args.serve_particles, max_systems=512,
                         max_steps_per_call=args.serve_chunk, law=args.law)
@@ -749,6 +757,7 @@ def run_serve(args):
                       log=lambda k, t: print("completed %d at %.1f s" % (k, t), file=sys.stderr)
                       if k and k % 100 == 0 else None)
         eng.close()
+        st["clocks"] = sampler.stop()
         out[pol] = st
     print(json.dumps(out), flush=True)
     return 0

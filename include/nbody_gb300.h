@@ -93,7 +93,11 @@ typedef struct nb_params {
     double mond_nu_index; /* MOND_nuIndex (reference default 2) */
     int32_t stages;       /* tuning override: depth of the force kernel's shared-memory ring of
                              j-tiles, 3, 4 or 6 (0 = 4) */
-    int32_t reserved;
+    int32_t resort_every; /* steps of nb_step / nb_step_until_output between Morton re-orders of
+                             the sources (0 = 16; 1 = every step).  Steps in between pack the
+                             sources in the last order, which stays a valid permutation: the
+                             forces differ only by FP32 round-off.  Every other force call,
+                             nb_upload and nb_checkpoint_load re-order first. */
 } nb_params;
 
 #define NB_BG_NONE 0
@@ -391,7 +395,8 @@ int nb_selftest_wait_timeout(int device, int64_t timeout_ns, double *waited_ms);
  * lane. */
 int nb_selftest_fp32_peak(int device, int packed, double *tflops, double *ms);
 
-/* Last error message of this handle (never NULL). */
+/* Last error message of this handle (never NULL).  With a NULL handle: why the
+ * last nb_create on the calling thread failed. */
 const char *nb_last_error(nb_handle *h);
 
 /* Library version string. */

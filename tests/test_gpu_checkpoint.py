@@ -74,3 +74,27 @@ def test_bad_images_are_rejected(nb):
         b.restore(bytes(bad))
     # the handle still works after the rejected loads
     nb.compute_force(b)
+
+
+def test_image_with_a_bad_source_order_loads_and_resorts(nb):
+    """The image keeps the step graphs' Morton permutation so that a restored
+    run continues bit-identically; a block that is not a permutation of
+    0..n-1 is dropped at load (the next step sorts again) instead of being
+    gathered through."""
+    n = 500
+    d = nb.plummer(n, seed=55)
+    kw = dict(ForceSofteningTable=[0.01] * 6, TimeStep=1e-3, TimeEnd=1.0, precision="mixed")
+    a = nb.Simulation(d, **kw)
+    nb.run(a, nsteps=3)
+    nb.step(a, 2)
+    img = bytearray(a.checkpoint())
+    perm = np.frombuffer(bytes(img[-4 * n:]), dtype=np.int32)
+    assert sorted(perm.tolist()) == list(range(n))
+    for bad_value in (n, -1, int(perm[1])):
+        bad = bytearray(img)
+        bad[-4 * n:-4 * n + 4] = np.int32(bad_value).tobytes()
+        b = nb.Simulation(d, **kw)
+        b.restore(bytes(bad))
+        nb.step(b, 4)
+        g = nb.get_all_data(b)
+        assert np.all(np.isfinite(g["pos"])) and np.all(np.isfinite(g["acc"]))

@@ -177,9 +177,10 @@ def test_adaptive_many_body_matches_oracle(nb, oracle):
 
 
 def test_step_graph_matches_single_calls(nb):
-    """nb_step's graph replay equals the same operations issued one by one."""
+    """nb_step's graph replay equals the same operations issued one by one
+    (with the sources re-ordered every step, as every nb_compute_force does)."""
     d = nb.plummer(5000, seed=3)
-    kw = dict(ForceSofteningTable=[0.01] * 6, TimeStep=1e-3, precision="mixed")
+    kw = dict(ForceSofteningTable=[0.01] * 6, TimeStep=1e-3, precision="mixed", resort_every=1)
     a = nb.Simulation(d, **kw)
     b = nb.Simulation(d, **kw)
     for s in (a, b):
@@ -195,6 +196,63 @@ def test_step_graph_matches_single_calls(nb):
     ga, gb = nb.get_all_data(a), nb.get_all_data(b)
     np.testing.assert_array_equal(ga["pos"], gb["pos"])
     np.testing.assert_array_equal(ga["vel"], gb["vel"])
+
+
+@pytest.mark.parametrize("resort", [0, 7])
+def test_step_graph_sort_interval(nb, resort):
+    """Steps between two Morton re-orders pack the sources in the last order:
+    the run matches the one that re-orders every step to FP32 round-off
+    (after 40 steps of dt 1e-3 on a Plummer sphere: position difference
+    <= 1e-9 of the system's extent, velocity difference <= 1e-6 of the
+    largest speed).  A second nb_step call and an upload in between keep the
+    order valid."""
+    d = nb.plummer(6000, seed=31)
+    kw = dict(ForceSofteningTable=[0.01] * 6, TimeStep=1e-3, precision="mixed")
+    a = nb.Simulation(d, resort_every=resort, **kw)
+    b = nb.Simulation(d, resort_every=1, **kw)
+    for s in (a, b):
+        nb.compute_force(s)
+        nb.leapfrog_half_kick(s, +1)
+        nb.step(s, 25)
+    # re-upload each run's own state (the clock restarts in both): the order of
+    # the next steps is rebuilt before the first replay
+    for s in (a, b):
+        g = nb.get_all_data(s)
+        s.upload({"pos": g["pos"], "vel": g["vel"], "mass": d["mass"]})
+        nb.step(s, 15)
+    ga, gb = nb.get_all_data(a), nb.get_all_data(b)
+    ext = np.ptp(gb["pos"], axis=0).max()
+    assert np.abs(ga["pos"] - gb["pos"]).max() <= 1e-9 * ext
+    vmax = np.linalg.norm(gb["vel"], axis=1).max()
+    assert np.abs(ga["vel"] - gb["vel"]).max() <= 1e-6 * vmax
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_upload_of_same_size_reuses_step_graphs(nb, precision):
+    """An upload of as many particles keeps the captured step graphs (they
+    hold pointers and counts, not data): stepping the new state gives the
+    same result, bit for bit, as a fresh handle holding it.  A smaller upload
+    re-captures them."""
+    kw = dict(ForceSofteningTable=[0.01] * 6, TimeStep=1e-3, precision=precision, resort_every=1)
+    a = nb.Simulation(nb.plummer(3000, seed=71), **kw)
+    nb.step(a, 4)
+    for n, seed in ((3000, 72), (1500, 73)):
+        d = nb.plummer(n, seed=seed)
+        a.upload(d)
+        nb.step(a, 6)
+        b = nb.Simulation(d, **kw)
+        nb.step(b, 6)
+        ga, gb = nb.get_all_data(a), nb.get_all_data(b)
+        np.testing.assert_array_equal(ga["pos"], gb["pos"])
+        np.testing.assert_array_equal(ga["vel"], gb["vel"])
+        b.close()
+
+
+def test_resort_every_validation(nb):
+    d = nb.plummer(64, seed=1)
+    for bad in (-1, (1 << 20) + 1):
+        with pytest.raises(Exception, match="resort_every"):
+            nb.Simulation(d, ForceSofteningTable=[0.01] * 6, TimeStep=1e-3, resort_every=bad)
 
 
 def test_collision_adaptive_mixed_vs_fp64(nb):
