@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(BLOCK, (ForceOcc<BLOCK, IPT, POT>::value)) k_f
         if (LAW == NB_LAW_SPLINE_G2) near = warp_near<IPT>(ex, xr, yr, zr, hh, pidx);
         if (near)
             pair_loop_checked<LAW, ACC, POT, IPT, TJ>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, ex.w);
-        else if (ex.w > 0.0f && warp_expandable<IPT>(oh.w, xr, yr, zr, pidx))
+        else if (ex.w > 0.0f && warp_expandable<IPT>(ex, oh.w, xr, yr, zr, pidx))
             pair_loop_expand<LAW, ACC, POT, IPT, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);
         else
             pair_loop_far<LAW, ACC, POT, IPT, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);

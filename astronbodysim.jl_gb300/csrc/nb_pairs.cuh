@@ -164,31 +164,43 @@ __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, con
 }
 
 // Far-tile loop in expanded form, for full uniform-mass tiles (the pack then
-// stores |q|^2 in each source's mass slot) seen from targets at least
-// kExpandRatio tile radii from the tile origin:
+// stores |q|^2 in each source's mass slot):
 //   r^2 = (|q|^2 + |x|^2 [+ h^2]) - 2 q.x            (4 FP32 operations)
 //   sum_j (q_j - x) r_j^-3 = sum_j q_j r_j^-3 - x sum_j r_j^-3
 // so the three differences q - x drop out of the pair loop: 10 FP32
-// operations per interaction instead of 11 (the MUFU rsqrt unchanged).  With
-// |x| >= 2.5 |q|, (|x|^2 + |q|^2) / |x - q|^2 <= 1.16 / 0.36 = 3.2, so the
-// rounding of r^2 (about 3 ulp of |x|^2 + |q|^2) stays within about 10 ulp of
-// r^2, and sum q r^-3 - x sum r^-3 cancels by at most 1.4 / 0.6 = 7/3.
-// (Measured at N = 2^20: median and p99 relative force errors 2.6e-8 and
-// 4.9e-7, as with the difference form alone.)
-#ifndef NB_EXPAND_RATIO
-#define NB_EXPAND_RATIO 2.5f
+// operations per interaction instead of 11 (the MUFU rsqrt unchanged).
+// Rounding: r^2 carries about 3 ulp of |q|^2 + |x|^2, and the two sums of the
+// acceleration cancel by at most (|q| + |x|) / r.  Both stay bounded when
+//   |q|^2 + |x|^2 <= (R^2 + |x|^2) <= kExpandBound * d^2
+// for every target of the warp, with R the tile radius (|q| <= R) and d the
+// distance from the target to the tile's box (r >= d; the box is enlarged
+// for rounding, so d never exceeds a true distance): the relative error of
+// r^2 stays within about 3 kExpandBound ulp and the cancellation within
+// sqrt(2 kExpandBound).  A target inside the box (d = 0) never qualifies.
+// The box distance admits more tiles than a test on |x| alone: at N = 2^20
+// (Plummer, tiles of 512) |x| >= 2.5 R (worst case 3.22) admits 76 % of the
+// (warp, tile) pairs, this test with the bound 3.25 84 % and with 5 90 %.
+// Bounds of 3.25, 5 and 8 gave the same force error quantiles against the
+// FP64 oracle at N = 2^20 (median 3.0e-8, p99 4.8e-7, max 1.76e-5).
+#ifndef NB_EXPAND_BOUND
+#define NB_EXPAND_BOUND 5.0f
 #endif
-constexpr float kExpandRatio = NB_EXPAND_RATIO;
+constexpr float kExpandBound = NB_EXPAND_BOUND;
 
 template <int IPT>
-__device__ __forceinline__ bool warp_expandable(float radius, const float* xr, const float* yr,
-                                                const float* zr, const int32_t* pidx) {
+__device__ __forceinline__ bool warp_expandable(const float4 e, float radius, const float* xr,
+                                                const float* yr, const float* zr,
+                                                const int32_t* pidx) {
     bool ok = true;
-    const float lim = kExpandRatio * radius;
+    const float rr = radius * radius;
 #pragma unroll
     for (int k = 0; k < IPT; ++k) {
+        const float bx = fmaxf(fabsf(xr[k]) - e.x, 0.0f);
+        const float by = fmaxf(fabsf(yr[k]) - e.y, 0.0f);
+        const float bz = fmaxf(fabsf(zr[k]) - e.z, 0.0f);
+        const float d2 = fmaf(bx, bx, fmaf(by, by, bz * bz));
         const float x2 = fmaf(xr[k], xr[k], fmaf(yr[k], yr[k], zr[k] * zr[k]));
-        ok &= (pidx[k] < 0) || (x2 >= lim * lim);
+        ok &= (pidx[k] < 0) || (x2 + rr <= kExpandBound * d2);
     }
     return __all_sync(0xffffffffu, ok);
 }
