@@ -367,6 +367,33 @@ struct BatchOcc {
         (ACC && !POT) ? (BLOCK == 128 ? (IPT == 1 ? 6 : 5) : (IPT == 1 ? 3 : 2)) : 1;
 };
 
+// v += a * (dt * fac) of one particle: fac 1 for a full kick, +-0.5 for the
+// leapfrog half kicks at admission and retirement (src/base/Timestep.jl:84-93,
+// 116-125), in the single-system kernels' operation order: a * dt for full
+// kicks, a * fw * 0.5 * dt for half kicks.  Used by k_batch_kick and by the
+// force kernel's fused kick, so both give the same bits.
+__device__ __forceinline__ void kick_particle(double* __restrict__ vx, double* __restrict__ vy,
+                                              double* __restrict__ vz, int64_t i, double ax,
+                                              double ay, double az, const int32_t* __restrict__ sysid,
+                                              const double* __restrict__ dt_slot,
+                                              const double* __restrict__ fac_slot) {
+    const int32_t s = sysid[i];
+    if (s < 0) return;
+    const double f = fac_slot[s];
+    if (f == 0.0) return;
+    const double dt = dt_slot[s];
+    if (f == 1.0) {
+        vx[i] = __dadd_rn(vx[i], __dmul_rn(ax, dt));
+        vy[i] = __dadd_rn(vy[i], __dmul_rn(ay, dt));
+        vz[i] = __dadd_rn(vz[i], __dmul_rn(az, dt));
+    } else {
+        const double fw = f > 0.0 ? 1.0 : -1.0;
+        vx[i] = __dadd_rn(vx[i], __dmul_rn(__dmul_rn(__dmul_rn(ax, fw), 0.5), dt));
+        vy[i] = __dadd_rn(vy[i], __dmul_rn(__dmul_rn(__dmul_rn(ay, fw), 0.5), dt));
+        vz[i] = __dadd_rn(vz[i], __dmul_rn(__dmul_rn(__dmul_rn(az, fw), 0.5), dt));
+    }
+}
+
 template <int LAW, bool ACC, bool POT, int BLOCK, int IPT>
 __global__ void __launch_bounds__(BLOCK, (BatchOcc<BLOCK, IPT, ACC, POT>::value))
     k_force_batch(BatchForce f) {
@@ -465,12 +492,14 @@ __global__ void __launch_bounds__(BLOCK, (BatchOcc<BLOCK, IPT, ACC, POT>::value)
             const float4 ex = f.ext[d.tile_off + t];
             bool near = false;
             if (LAW == NB_LAW_SPLINE_G2) near = warp_near<IPT>(ex, xr, yr, zr, hh, pidx);
+            // the system's last tile may be partial
+            const int np2 = tile_pairs<kTileJ>(d.n - t * kTileJ);
             if (near)
-                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, ex.w);
+                pair_loop_checked<LAW, ACC, POT, IPT>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, ex.w, np2);
             else if (ex.w > 0.0f && warp_expandable<IPT>(ex, oh.w, xr, yr, zr, pidx))
                 pair_loop_expand<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);
             else
-                pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w);
+                pair_loop_far<LAW, ACC, POT, IPT>(b, xr, yr, zr, h2, ax, ay, az, ap, ex.w, np2);
             __syncwarp();
             if (lane == 0) {
                 __threadfence_block();
@@ -502,9 +531,13 @@ __global__ void __launch_bounds__(BLOCK, (BatchOcc<BLOCK, IPT, ACC, POT>::value)
                 const int32_t p = pidx[k];
                 if (p < 0) continue;
                 if (ACC) {
-                    f.ax[p] = ((double)sx[k] + (double)cx[k]) * f.G;
-                    f.ay[p] = ((double)sy[k] + (double)cy[k]) * f.G;
-                    f.az[p] = ((double)sz[k] + (double)cz[k]) * f.G;
+                    const double a0 = ((double)sx[k] + (double)cx[k]) * f.G;
+                    const double a1 = ((double)sy[k] + (double)cy[k]) * f.G;
+                    const double a2 = ((double)sz[k] + (double)cz[k]) * f.G;
+                    f.ax[p] = a0;
+                    f.ay[p] = a1;
+                    f.az[p] = a2;
+                    if (f.vx) kick_particle(f.vx, f.vy, f.vz, p, a0, a1, a2, f.sysid, f.dt_slot, f.fac_slot);
                 }
                 if (POT) {
                     double phi = -((double)sp[k] + (double)cp[k]);
@@ -611,8 +644,8 @@ __global__ void __launch_bounds__(kBThreads)
     z[i] = __dadd_rn(z[i], __dmul_rn(vz[i], dt));
 }
 
-// v += a * (dt * fac): fac 1 for a full kick, +-0.5 for the leapfrog half
-// kicks at admission and retirement (src/base/Timestep.jl:84-93, 116-125).
+// v += a * (dt * fac) over the arena (the admission and retirement half kicks;
+// the step's full kick is fused into k_force_batch).
 __global__ void __launch_bounds__(kBThreads)
     k_batch_kick(double* __restrict__ vx, double* __restrict__ vy, double* __restrict__ vz,
                  const double* __restrict__ ax, const double* __restrict__ ay,
@@ -621,24 +654,7 @@ __global__ void __launch_bounds__(kBThreads)
                  int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
     if (i >= n) return;
-    const int32_t s = sysid[i];
-    if (s < 0) return;
-    const double f = fac_slot[s];
-    if (f == 0.0) return;
-    // Same operation order as the single-system kernels: a * fw * 0.5 * dt for
-    // half kicks, a * dt for full kicks.
-    if (f == 1.0) {
-        const double dt = dt_slot[s];
-        vx[i] = __dadd_rn(vx[i], __dmul_rn(ax[i], dt));
-        vy[i] = __dadd_rn(vy[i], __dmul_rn(ay[i], dt));
-        vz[i] = __dadd_rn(vz[i], __dmul_rn(az[i], dt));
-    } else {
-        const double fw = f > 0.0 ? 1.0 : -1.0;
-        const double dt = dt_slot[s];
-        vx[i] = __dadd_rn(vx[i], __dmul_rn(__dmul_rn(__dmul_rn(ax[i], fw), 0.5), dt));
-        vy[i] = __dadd_rn(vy[i], __dmul_rn(__dmul_rn(__dmul_rn(ay[i], fw), 0.5), dt));
-        vz[i] = __dadd_rn(vz[i], __dmul_rn(__dmul_rn(__dmul_rn(az[i], fw), 0.5), dt));
-    }
+    kick_particle(vx, vy, vz, i, ax[i], ay[i], az[i], sysid, dt_slot, fac_slot);
 }
 
 __global__ void k_fill_i32(int32_t* __restrict__ a, int64_t n, int32_t v) {

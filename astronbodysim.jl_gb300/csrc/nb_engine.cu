@@ -322,11 +322,17 @@ cudaError_t enqueue_step(nb_engine* e, cudaStream_t s) {
     if (r != cudaSuccess) return r;
     r = enqueue_sort_pack(e, s, false);
     if (r != cudaSuccess) return r;
-    r = nb::launch_force_batch(e->p.law, force_args(e, e->items, e->nitems), e->occ_acc * e->nsm,
-                               e->fblock, e->fipt, s);
-    if (r != cudaSuccess) return r;
-    r = nb::launch_batch_kick(e->vx, e->vy, e->vz, e->ax, e->ay, e->az, e->sysid, e->dt_slot,
-                              e->fac_step, e->high_water, s);
+    // force with the step's kick fused into its epilogue: every target of the
+    // work items is a particle of a running system, and those are exactly
+    // the particles the kick moves (fac_step 1)
+    nb::BatchForce f = force_args(e, e->items, e->nitems);
+    f.vx = e->vx;
+    f.vy = e->vy;
+    f.vz = e->vz;
+    f.sysid = e->sysid;
+    f.dt_slot = e->dt_slot;
+    f.fac_slot = e->fac_step;
+    r = nb::launch_force_batch(e->p.law, f, e->occ_acc * e->nsm, e->fblock, e->fipt, s);
     if (r != cudaSuccess) return r;
     return nb::launch_batch_tick(e->batchsys, e->nrank, e->steps_slot, s);
 }

@@ -220,6 +220,15 @@ struct BatchForce {
     double* pot;
     double G;
     uint32_t* err;
+    // Optional kick fused into the epilogue (the engine's step): with vx set,
+    // each target's velocity takes v += a * dt_slot[s] * fac_slot[s] exactly
+    // as k_batch_kick would apply it right after the force (s = sysid[p]).
+    double* vx;
+    double* vy;
+    double* vz;
+    const int32_t* sysid;
+    const double* dt_slot;
+    const double* fac_slot;
 };
 
 cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, int block, int ipt,

@@ -96,7 +96,7 @@ template <int LAW, bool ACC, bool POT, int IPT, bool UNI = false, int TJ = kTile
 __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, const float* xr,
                                                const float* yr, const float* zr, const float* h2,
                                                float* ax, float* ay, float* az, float* ap,
-                                               float mu = 1.0f) {
+                                               float mu = 1.0f, int np2 = TJ / 2) {
     // With one target per thread the sums are split over two sets (even and
     // odd source pairs) so that consecutive accumulating FMAs do not wait on
     // each other; with more targets per thread they are independent already.
@@ -113,7 +113,7 @@ __device__ __forceinline__ void pair_loop_fast(const float4* __restrict__ b, con
         for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
 #pragma unroll (LoopShape<IPT>::UNROLL)
-    for (int p = 0; p < TJ / 2; p += NA) {
+    for (int p = 0; p < np2; p += NA) {
 #pragma unroll
         for (int u = 0; u < NA; ++u) {
             const float4 A = b[2 * (p + u)];
@@ -269,24 +269,37 @@ __device__ __forceinline__ void pair_loop_expand(const float4* __restrict__ b, c
     }
 }
 
+// Source pairs of a tile the loops visit: the tile's real sources rounded up
+// to 16 (the pair loops' step).  The zero-mass padding beyond them adds
+// exactly 0 (its r^-3 underflows and its potential term is m r^-1 = 0), so
+// stopping there leaves every sum bit-identical and saves the padding's
+// share of a partial tile: about 3 % of the interactions evaluated in an
+// ensemble of systems of 64 .. 8192 particles with tiles of 256.
+template <int TJ>
+__device__ __forceinline__ int tile_pairs(int count) {
+    return count >= TJ ? TJ / 2 : (count + 15) / 16 * 8;
+}
+
 // Far-tile dispatch: the uniform-mass loop when the pack flagged the tile.
 template <int LAW, bool ACC, bool POT, int IPT, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_far(const float4* __restrict__ b, const float* xr,
                                               const float* yr, const float* zr, const float* h2,
-                                              float* ax, float* ay, float* az, float* ap, float mu) {
+                                              float* ax, float* ay, float* az, float* ap, float mu,
+                                              int np2 = TJ / 2) {
     // mu < 0: uniform but partial tile (usable for the acceleration only)
     const float m = POT ? mu : fabsf(mu);
     if (m > 0.0f)
-        pair_loop_fast<LAW, ACC, POT, IPT, true, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap, m);
+        pair_loop_fast<LAW, ACC, POT, IPT, true, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap, m, np2);
     else
-        pair_loop_fast<LAW, ACC, POT, IPT, false, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap);
+        pair_loop_fast<LAW, ACC, POT, IPT, false, TJ>(b, xr, yr, zr, h2, ax, ay, az, ap, 1.0f, np2);
 }
 
 template <int LAW, bool ACC, bool POT, int IPT, bool UNI, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict__ b, const float* xr,
                                                        const float* yr, const float* zr,
                                                        const float* hh, const float* h2, float* ax,
-                                                       float* ay, float* az, float* ap, float mu) {
+                                                       float* ay, float* az, float* ap, float mu,
+                                                       int np2) {
     // Two passes over the tile.  Pass 1 is the packed FP32x2 loop of
     // pair_loop_fast (uniform-mass form and split sums included) on r^2
     // clamped to at least h^2: a pair with r < h adds the bounded Newtonian
@@ -310,7 +323,7 @@ __device__ __forceinline__ void pair_loop_checked_impl(const float4* __restrict_
         for (int u = 0; u < NA; ++u) sx[u][k] = sy[u][k] = sz[u][k] = sp[u][k] = make_float2(0.0f, 0.0f);
     }
 #pragma unroll 1
-    for (int q = 0; q < TJ / 16; ++q) {
+    for (int q = 0; q < np2 / 8; ++q) {
         float rmin[IPT];
 #pragma unroll
         for (int k = 0; k < IPT; ++k) rmin[k] = 3e38f;
@@ -429,12 +442,14 @@ template <int LAW, bool ACC, bool POT, int IPT, int TJ = kTileJ>
 __device__ __forceinline__ void pair_loop_checked(const float4* __restrict__ b, const float* xr,
                                                   const float* yr, const float* zr,
                                                   const float* hh, const float* h2, float* ax,
-                                                  float* ay, float* az, float* ap, float mu) {
+                                                  float* ay, float* az, float* ap, float mu,
+                                                  int np2 = TJ / 2) {
     const float m = POT ? mu : fabsf(mu);
     if (m > 0.0f)
-        pair_loop_checked_impl<LAW, ACC, POT, IPT, true, TJ>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, m);
+        pair_loop_checked_impl<LAW, ACC, POT, IPT, true, TJ>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, m, np2);
     else
-        pair_loop_checked_impl<LAW, ACC, POT, IPT, false, TJ>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, 1.0f);
+        pair_loop_checked_impl<LAW, ACC, POT, IPT, false, TJ>(b, xr, yr, zr, hh, h2, ax, ay, az, ap, 1.0f,
+                                                              np2);
 }
 
 }  // namespace nb
