@@ -18,12 +18,12 @@
 //   * calls whose work overlaps on the GPU (other streams, other host threads)
 //     race on it and corrupt each other's results -- serialise them.
 // Set-up: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress while that device is current and caches it; that first
-// call should come before any stream capture.  Later calls check the cached
+// cudaGetSymbolAddress while that device is current and caches it.  Every
+// call reads the error word back and synchronises its stream, so no call can
+// run inside a stream capture.  Later calls check the cached
 // address with cudaPointerGetAttributes (no allocation) and repeat the set-up
 // when it no longer names device memory of the current device -- after a
-// cudaDeviceReset, which ends the context the address belonged to.  Every
-// call synchronises its stream before it returns.
+// cudaDeviceReset, which ends the context the address belonged to.
 #include <cstdio>
 #include <cstring>
 #include <mutex>

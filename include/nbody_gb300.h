@@ -287,8 +287,9 @@ int nb_checkpoint_load(nb_handle *h, const void *buf, int64_t bytes);
  * (about 2.7 MB, held by every GPU that loads the library until exit), so
  * n must be 1..65536; larger n returns NB_ERR_INVALID_ARG with a message in
  * errbuf (may be NULL).  All calls share that array: calls that overlap on the
- * GPU race and must be serialised by the caller.  The first call on a device
- * looks up the array's address and should come before any stream capture.
+ * GPU race and must be serialised by the caller.  Every call reads an error
+ * word back and synchronises its stream, so no call can run inside a stream
+ * capture.
  * Results agree with nb_compute_force of a handle with NB_PREC_MIXED, the same
  * law, G and softening for every particle type, within the mixed-precision
  * tolerance: the same kernels, with another launch shape (128 threads x 2
