@@ -113,7 +113,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_oracle_rate(data, n_targets, seed=7, nthreads=0):
+def cpu_oracle_rate(data, n_targets, seed=7, nthreads=0, law="spline"):
     """Oracle (CPU Float64 restatement of src/directsum/gravity.jl:37-46, 80-101)
     on a bounded sample: n_targets seeded targets x all sources."""
     from oracle import oracle
@@ -122,7 +122,8 @@ def cpu_oracle_rate(data, n_targets, seed=7, nthreads=0):
     idx = rng.choice(data["pos"].shape[0], size=n_targets, replace=False)
     t0 = time.perf_counter()
     oracle.force(data["pos"], data["mass"], data["pos"][idx], EPS, want_pot=False,
-                 nthreads=nthreads)
+                 nthreads=nthreads,
+                 law=oracle.LAW_SPLINE_G2 if law == "spline" else oracle.LAW_PLUMMER)
     dt = time.perf_counter() - t0
     return n_targets * data["pos"].shape[0] / dt, dt, oracle.max_threads() if nthreads == 0 else nthreads
 
@@ -303,10 +304,10 @@ def run_reference(args):
     data = nb.plummer(n, seed=2)
     targets = args.ref_targets
     for _ in range(args.warmup):
-        cpu_oracle_rate(data, targets)
+        cpu_oracle_rate(data, targets, law=args.law)
     total_pairs, total_t, cores = 0.0, 0.0, 1
     for k in range(args.steps):
-        rate, dt, cores = cpu_oracle_rate(data, targets, seed=100 + k)
+        rate, dt, cores = cpu_oracle_rate(data, targets, seed=100 + k, law=args.law)
         total_pairs += rate * dt
         total_t += dt
     v = total_pairs / total_t / 1e9
@@ -315,8 +316,13 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Plummer sphere)",
-        "config": {"workload": "plummer_n%d_eps1e-3_spline" % n, "n": n,
-                   "sample": "%d seeded targets x %d sources per step" % (targets, n)},
+        # the native arm's workload, each step a bounded sample of it: the
+        # reference's CPU direct sum (FP64) of seeded targets against all N
+        # sources, i.e. the N^2 force that dominates a KDK step
+        "config": {"workload": "plummer_n%d_eps1e-3_%s_mixed_kdk_dt1e-4" % (n, args.law), "n": n,
+                   "law": args.law,
+                   "sample": "%d seeded targets x %d sources per step, FP64 force only (the O(N) "
+                             "kick and drift of a step are not timed)" % (targets, n)},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "%d targets x %d sources per step, OpenMP static blocks" % (targets, n)},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -523,7 +529,7 @@ def run_gpu(args):
                 traffic = None
         cpu = None
         if not args.skip_cpu_baseline:
-            rate, dt, cores = cpu_oracle_rate(data, args.cpu_targets)
+            rate, dt, cores = cpu_oracle_rate(data, args.cpu_targets, law=args.law)
             cpu = {"value": rate / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
                    "sample": "%d seeded targets x %d sources (%.1f s), OpenMP static blocks, FP64"
                              % (args.cpu_targets, n, dt)}
