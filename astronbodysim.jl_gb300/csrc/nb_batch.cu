@@ -101,7 +101,8 @@ constexpr int kSortCta = 1024;
 
 __global__ void __launch_bounds__(kSortCta)
     k_batch_sort_small(const BatchSys* __restrict__ bs, const int64_t* __restrict__ steps_slot,
-                       int32_t every, int32_t force_all, const double* __restrict__ x,
+                       const int64_t* __restrict__ nsteps_slot, int32_t every, int32_t force_all,
+                       const double* __restrict__ x,
                        const double* __restrict__ y, const double* __restrict__ z,
                        double* __restrict__ bbox, int32_t* __restrict__ lperm) {
     extern __shared__ uint64_t sk[];
@@ -111,6 +112,8 @@ __global__ void __launch_bounds__(kSortCta)
     // Re-ordered at admission and every `every` of the system's own steps, so
     // the schedule does not depend on the other systems.
     if (!force_all && steps_slot[d.slot] % every != 0) return;
+    // a system that has made all its steps keeps its order (and positions)
+    if (!force_all && nsteps_slot && steps_slot[d.slot] >= nsteps_slot[d.slot]) return;
     const int tid = threadIdx.x;
     double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
     for (int i = tid; i < d.n; i += kSortCta) {
@@ -195,10 +198,14 @@ __global__ void __launch_bounds__(kBThreads)
 }
 
 // Per-system step counter (drives the re-ordering schedule).
+// A system whose count has reached its target (nsteps_slot) stops counting.
 __global__ void k_batch_tick(const BatchSys* __restrict__ bs, int32_t nrank,
-                             int64_t* __restrict__ steps_slot) {
+                             int64_t* __restrict__ steps_slot,
+                             const int64_t* __restrict__ nsteps_slot) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < nrank) steps_slot[bs[r].slot] += 1;
+    if (r >= nrank) return;
+    const int32_t s = bs[r].slot;
+    if (!nsteps_slot || steps_slot[s] < nsteps_slot[s]) steps_slot[s] += 1;
 }
 
 int batch_small_sort_limit() { return kSmallSort; }
@@ -209,14 +216,15 @@ cudaError_t prepare_batch_sort_small() {
 }
 
 cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t max_small_n,
-                                    const int64_t* steps_slot, int32_t every, int32_t force_all,
-                                    const double* x, const double* y, const double* z,
-                                    double* bbox, int32_t* lperm, cudaStream_t s) {
+                                    const int64_t* steps_slot, const int64_t* nsteps_slot,
+                                    int32_t every, int32_t force_all, const double* x,
+                                    const double* y, const double* z, double* bbox, int32_t* lperm,
+                                    cudaStream_t s) {
     if (nrank <= 0 || max_small_n <= 0) return cudaSuccess;
     int np2 = 1;
     while (np2 < max_small_n) np2 <<= 1;
-    k_batch_sort_small<<<nrank, kSortCta, sizeof(uint64_t) * np2, s>>>(bs, steps_slot, every, force_all,
-                                                                        x, y, z, bbox, lperm);
+    k_batch_sort_small<<<nrank, kSortCta, sizeof(uint64_t) * np2, s>>>(bs, steps_slot, nsteps_slot, every,
+                                                                        force_all, x, y, z, bbox, lperm);
     return cudaGetLastError();
 }
 
@@ -227,9 +235,10 @@ cudaError_t launch_batch_perm_to_local(const BatchSys* bs, int32_t nrank, const 
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_tick(const BatchSys* bs, int32_t nrank, int64_t* steps_slot, cudaStream_t s) {
+cudaError_t launch_batch_tick(const BatchSys* bs, int32_t nrank, int64_t* steps_slot,
+                              const int64_t* nsteps_slot, cudaStream_t s) {
     if (nrank <= 0) return cudaSuccess;
-    k_batch_tick<<<(nrank + 255) / 256, 256, 0, s>>>(bs, nrank, steps_slot);
+    k_batch_tick<<<(nrank + 255) / 256, 256, 0, s>>>(bs, nrank, steps_slot, nsteps_slot);
     return cudaGetLastError();
 }
 
@@ -241,18 +250,29 @@ __global__ void __launch_bounds__(kTileJ)
                  const double* __restrict__ x, const double* __restrict__ y,
                  const double* __restrict__ z, const double* __restrict__ m,
                  float4* __restrict__ pack, TileOrigin* __restrict__ origin,
-                 float4* __restrict__ ext) {
-    // The tile's bounding box is reduced in FP32 relative to the tile's first
-    // particle c (FP64); the tile origin is c + float offset, and the sources
-    // are re-expressed relative to it from their FP64 offsets to c.  The
-    // common-mass test compares bit patterns.  FP64 work (slow on this GPU) is
-    // kept to the offsets.  Everything depends on this tile's particles only.
+                 float4* __restrict__ ext, const int32_t* __restrict__ sysid,
+                 const int64_t* __restrict__ steps_slot, const int64_t* __restrict__ nsteps_slot) {
+    // Each particle is split once into a double-float pair (the FP64 work of
+    // this kernel, slow on this GPU: 12 FP64-pipe operations per particle).
+    // The tile's bounding box is reduced in FP32 from the pairs relative to
+    // the tile's first particle c; thread 0 alone forms the tile origin c +
+    // float offset in FP64 and shares it.  Sources are re-expressed relative
+    // to it from their pairs by the steps the force kernel applies to targets.
+    // The common-mass test compares bit patterns.  Everything depends on this
+    // tile's particles only.
     __shared__ float red[6][kTileJ / 32];
     __shared__ double cref[4];
+    __shared__ float2 csplit[3];
+    __shared__ TileOrigin tile_o;
     const int32_t g = blockIdx.x;
     const int32_t r = tile_rank[g];
     const SysDesc& d = sys[r];
     (void)bbox;
+    if (nsteps_slot) {
+        // a system that has made all its steps is skipped by the force too
+        const int32_t s = sysid[d.off];
+        if (steps_slot[s] >= nsteps_slot[s]) return;  // CTA-uniform
+    }
     const int32_t t = g - d.tile_off;
     const int32_t slot = t * kTileJ + threadIdx.x;
     const bool valid = slot < d.n;
@@ -264,16 +284,23 @@ __global__ void __launch_bounds__(kTileJ)
         pz = z[p];
         pm = m[p];
     }
+    const float2 sx = split_df(px), sy = split_df(py), sz = split_df(pz);
     if (threadIdx.x == 0) {
         cref[0] = px;
         cref[1] = py;
         cref[2] = pz;
         cref[3] = pm;
+        csplit[0] = sx;
+        csplit[1] = sy;
+        csplit[2] = sz;
     }
     __syncthreads();
-    const double cx = cref[0], cy = cref[1], cz = cref[2], m0 = cref[3];
-    const double dx = px - cx, dy = py - cy, dz = pz - cz;
-    const float fx = (float)dx, fy = (float)dy, fz = (float)dz;
+    const double m0 = cref[3];
+    // offsets from c for the box (within a few FP32 ulp of the FP64 offsets;
+    // the box is enlarged below to cover that)
+    const float fx = rel_df(sx, csplit[0].x, csplit[0].y);
+    const float fy = rel_df(sy, csplit[1].x, csplit[1].y);
+    const float fz = rel_df(sz, csplit[2].x, csplit[2].y);
     const bool same_mass = !valid || __double_as_longlong(pm) == __double_as_longlong(m0);
     float v[6];
     v[0] = valid ? fx : 3e38f;
@@ -304,17 +331,21 @@ __global__ void __launch_bounds__(kTileJ)
         lo[k] = a;
         hi[k] = -b;
     }
-    const float oxf = 0.5f * (lo[0] + hi[0]), oyf = 0.5f * (lo[1] + hi[1]), ozf = 0.5f * (lo[2] + hi[2]);
-    const double oxd = (double)oxf, oyd = (double)oyf, ozd = (double)ozf;
-    TileOrigin to = make_tile_origin(cx + oxd, cy + oyd, cz + ozd, 0.0);
+    if (threadIdx.x == 0) {
+        const float oxf = 0.5f * (lo[0] + hi[0]), oyf = 0.5f * (lo[1] + hi[1]),
+                    ozf = 0.5f * (lo[2] + hi[2]);
+        tile_o = make_tile_origin(cref[0] + (double)oxf, cref[1] + (double)oyf, cref[2] + (double)ozf, 0.0);
+    }
+    __syncthreads();
+    TileOrigin to = tile_o;
     // Sources relative to the origin by the same FP32 steps the force kernel
     // applies to targets (rel_df): a particle's own entry and its target
     // coordinates are bit-identical, so the self pair has r = 0.
     float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
     if (valid) {
-        qx = rel_df(split_df(px), to.hi.x, to.lo.x);
-        qy = rel_df(split_df(py), to.hi.y, to.lo.y);
-        qz = rel_df(split_df(pz), to.hi.z, to.lo.z);
+        qx = rel_df(sx, to.hi.x, to.lo.x);
+        qy = rel_df(sy, to.hi.y, to.lo.y);
+        qz = rel_df(sz, to.hi.z, to.lo.z);
         qm = (float)pm;
     }
     // A full tile of one common mass keeps that mass in ext.w only; its mass
@@ -427,6 +458,15 @@ __global__ void __launch_bounds__(BLOCK, (BatchOcc<BLOCK, IPT, ACC, POT>::value)
         if (it >= f.nitems || abort_sh) break;  // CTA-uniform
         const int2 ib = f.items[it];
         const SysDesc& d = f.sys[ib.x];
+        if (f.nsteps_slot) {
+            // a system that has made all its steps keeps its state: no force,
+            // no kick (CTA-uniform: every thread reads the same words)
+            const int32_t s = f.sysid[d.off];
+            if (f.steps_slot[s] >= f.nsteps_slot[s]) {
+                __syncthreads();  // every thread has read item_sh
+                continue;
+            }
+        }
         const int32_t ntiles = d.ntiles;
         if (tid == 0) {
             for (int k = 0; k < kStages && k < ntiles; ++k) {
@@ -631,6 +671,7 @@ __global__ void __launch_bounds__(kBThreads)
                   const double* __restrict__ vx, const double* __restrict__ vy,
                   const double* __restrict__ vz, const int32_t* __restrict__ sysid,
                   const double* __restrict__ dt_slot, const double* __restrict__ fac_slot,
+                  const int64_t* __restrict__ steps_slot, const int64_t* __restrict__ nsteps_slot,
                   int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
     if (i >= n) return;
@@ -638,6 +679,7 @@ __global__ void __launch_bounds__(kBThreads)
     if (s < 0) return;
     const double f = fac_slot[s];
     if (f == 0.0) return;
+    if (nsteps_slot && steps_slot[s] >= nsteps_slot[s]) return;  // all steps made
     const double dt = __dmul_rn(dt_slot[s], f);
     x[i] = __dadd_rn(x[i], __dmul_rn(vx[i], dt));
     y[i] = __dadd_rn(y[i], __dmul_rn(vy[i], dt));
@@ -687,18 +729,22 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
                               const double* bbox, const int32_t* perm, const double* x,
                               const double* y, const double* z, const double* m, float4* pack,
-                              TileOrigin* origin, float4* ext, cudaStream_t s) {
+                              TileOrigin* origin, float4* ext, const int32_t* sysid,
+                              const int64_t* steps_slot, const int64_t* nsteps_slot,
+                              cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
-    k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, bbox, perm, x, y, z, m, pack, origin, ext);
+    k_batch_pack<<<ntiles, kTileJ, 0, s>>>(tile_rank, sys, bbox, perm, x, y, z, m, pack, origin, ext,
+                                           sysid, steps_slot, nsteps_slot);
     return cudaGetLastError();
 }
 
 cudaError_t launch_batch_drift(double* x, double* y, double* z, const double* vx, const double* vy,
                                const double* vz, const int32_t* sysid, const double* dt_slot,
-                               const double* fac_slot, int64_t n, cudaStream_t s) {
+                               const double* fac_slot, const int64_t* steps_slot,
+                               const int64_t* nsteps_slot, int64_t n, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     k_batch_drift<<<(unsigned)((n + kBThreads - 1) / kBThreads), kBThreads, 0, s>>>(
-        x, y, z, vx, vy, vz, sysid, dt_slot, fac_slot, n);
+        x, y, z, vx, vy, vz, sysid, dt_slot, fac_slot, steps_slot, nsteps_slot, n);
     return cudaGetLastError();
 }
 

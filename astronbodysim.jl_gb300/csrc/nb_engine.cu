@@ -10,9 +10,10 @@
 //     rebuilt whenever the set of running systems changes, and the step graph
 //     is re-captured then;
 //   * a step advances every running system by one KDK step; nb_engine_run
-//     replays the graph min(remaining steps, max_steps_per_call) times, so no
-//     system overshoots its step count, then retires finished systems and
-//     admits queued ones.
+//     replays the graph up to max_steps_per_call times; a per-slot gate on
+//     the device holds each system once it has made its step count, so none
+//     overshoots, and the call then retires finished systems and admits
+//     queued ones.
 // Each system follows run(sim) (src/run.jl:76-87, 101-173): force and +1/2
 // kick on admission, nsteps x (drift, force, kick), -1/2 kick on retirement.
 #include <algorithm>
@@ -76,6 +77,7 @@ struct nb_engine {
     int32_t* perm = nullptr;    // global radix-sort result (sorted slot -> arena particle)
     int32_t* lperm = nullptr;   // per-system Morton order, arena-relative
     int64_t* steps_slot = nullptr;
+    int64_t* nsteps_slot = nullptr;  // target own-step count of each running slot (0 otherwise)
     void* sort_scratch = nullptr;
     float4* pack = nullptr;
     nb::TileOrigin* origin = nullptr;
@@ -109,7 +111,8 @@ struct nb_engine {
     double pairs_per_step = 0.0;
     int32_t max_small_n = 0;   // largest system ordered in shared memory
     bool global_sort = false;  // some system is too large for the shared-memory sort
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;        // step graph without the per-slot gate
+    cudaGraphExec_t graph_gated = nullptr;  // with it, for chunks some system finishes inside
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     nb_engine_stats stats{};
     std::vector<int64_t> finished;  // ids retired since the last nb_engine_drain_done
@@ -177,6 +180,10 @@ void drop_graph(nb_engine* e) {
         cudaGraphExecDestroy(e->graph);
         e->graph = nullptr;
     }
+    if (e->graph_gated) {
+        cudaGraphExecDestroy(e->graph_gated);
+        e->graph_gated = nullptr;
+    }
 }
 
 int check_err(nb_engine* e) {
@@ -202,6 +209,7 @@ int rebuild(nb_engine* e) {
     std::vector<int32_t> ros(e->p.max_systems, -1);
     std::vector<int32_t> trank;
     std::vector<double> fstep(e->p.max_systems, 0.0), dts(e->p.max_systems, 0.0);
+    std::vector<int64_t> nst(e->p.max_systems, 0);
     int64_t soff = 0, toff = 0, hw = 0;
     double pairs = 0.0;
     for (int32_t r = 0; r < R; ++r) {
@@ -222,6 +230,7 @@ int rebuild(nb_engine* e) {
         for (int64_t t = 0; t < nt; ++t) trank.push_back(r);
         fstep[slots[r]] = 1.0;
         dts[slots[r]] = q.dt;
+        nst[slots[r]] = q.nsteps;
         soff += q.n;
         toff += nt;
         hw = std::max(hw, q.aoff + q.n);
@@ -246,6 +255,7 @@ int rebuild(nb_engine* e) {
     NE_CK(cudaMemcpy(e->rank_of_slot, ros.data(), sizeof(int32_t) * ros.size(), cudaMemcpyHostToDevice));
     NE_CK(cudaMemcpy(e->fac_step, fstep.data(), sizeof(double) * fstep.size(), cudaMemcpyHostToDevice));
     NE_CK(cudaMemcpy(e->dt_slot, dts.data(), sizeof(double) * dts.size(), cudaMemcpyHostToDevice));
+    NE_CK(cudaMemcpy(e->nsteps_slot, nst.data(), sizeof(int64_t) * nst.size(), cudaMemcpyHostToDevice));
     e->nrank = R;
     e->ntiles_total = (int32_t)toff;
     e->nitems = (int32_t)items.size();
@@ -293,7 +303,10 @@ nb::BatchForce force_args(nb_engine* e, const int2* items, int32_t nitems) {
 // larger systems are ordered every step by the global radix sort over the
 // arena, which runs only when such a system is resident.  Tile origins and
 // radii are recomputed from the current positions every step.
-cudaError_t enqueue_sort_pack(nb_engine* e, cudaStream_t s, bool force_all) {
+// gate: inside the step graph, skip the systems that have made all their
+// steps (at admission every new system is ordered and packed).
+cudaError_t enqueue_sort_pack(nb_engine* e, cudaStream_t s, bool force_all, bool gate) {
+    const int64_t* nsteps = gate ? e->nsteps_slot : nullptr;
     cudaError_t r = cudaSuccess;
     if (e->global_sort) {
         r = nb::launch_batch_bbox(e->batchsys, e->nrank, e->x, e->y, e->z, e->bbox, s);
@@ -307,20 +320,25 @@ cudaError_t enqueue_sort_pack(nb_engine* e, cudaStream_t s, bool force_all) {
         r = nb::launch_batch_perm_to_local(e->batchsys, e->nrank, e->perm, e->lperm, s);
         if (r != cudaSuccess) return r;
     }
-    r = nb::launch_batch_sort_small(e->batchsys, e->nrank, e->max_small_n, e->steps_slot,
+    r = nb::launch_batch_sort_small(e->batchsys, e->nrank, e->max_small_n, e->steps_slot, nsteps,
                                     kResortEvery, force_all ? 1 : 0, e->x, e->y, e->z, e->bbox,
                                     e->lperm, s);
     if (r != cudaSuccess) return r;
     return nb::launch_batch_pack(e->tile_rank, e->ntiles_total, e->sysdesc, e->bbox, e->lperm, e->x,
-                                 e->y, e->z, e->m, e->pack, e->origin, e->ext, s);
+                                 e->y, e->z, e->m, e->pack, e->origin, e->ext, e->sysid,
+                                 e->steps_slot, nsteps, s);
 }
 
-// One KDK step of every running system (enqueue only).
-cudaError_t enqueue_step(nb_engine* e, cudaStream_t s) {
+// One KDK step of every running system (enqueue only).  gated: hold the
+// systems that have made all their steps (a chunk that some system finishes
+// inside); without it every running system steps (and no kernel reads the
+// step counts).
+cudaError_t enqueue_step(nb_engine* e, cudaStream_t s, bool gated) {
+    const int64_t* nsteps = gated ? e->nsteps_slot : nullptr;
     cudaError_t r = nb::launch_batch_drift(e->x, e->y, e->z, e->vx, e->vy, e->vz, e->sysid, e->dt_slot,
-                                           e->fac_step, e->high_water, s);
+                                           e->fac_step, e->steps_slot, nsteps, e->high_water, s);
     if (r != cudaSuccess) return r;
-    r = enqueue_sort_pack(e, s, false);
+    r = enqueue_sort_pack(e, s, false, gated);
     if (r != cudaSuccess) return r;
     // force with the step's kick fused into its epilogue: every target of the
     // work items is a particle of a running system, and those are exactly
@@ -332,9 +350,11 @@ cudaError_t enqueue_step(nb_engine* e, cudaStream_t s) {
     f.sysid = e->sysid;
     f.dt_slot = e->dt_slot;
     f.fac_slot = e->fac_step;
+    f.steps_slot = e->steps_slot;
+    f.nsteps_slot = nsteps;
     r = nb::launch_force_batch(e->p.law, f, e->occ_acc * e->nsm, e->fblock, e->fipt, s);
     if (r != cudaSuccess) return r;
-    return nb::launch_batch_tick(e->batchsys, e->nrank, e->steps_slot, s);
+    return nb::launch_batch_tick(e->batchsys, e->nrank, e->steps_slot, nsteps, s);
 }
 
 // Admit queued requests (FIFO) while a slot and a particle range are free;
@@ -414,7 +434,7 @@ int start_systems(nb_engine* e, const std::vector<int32_t>& slots) {
     NE_CK(cudaMemcpy(e->items_new, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice));
     // New systems have step count 0, so they are due for ordering; the others
     // keep their order (their schedule must not depend on admissions).
-    NE_CK(enqueue_sort_pack(e, e->stream, false));
+    NE_CK(enqueue_sort_pack(e, e->stream, false, false));
     NE_CK(nb::launch_force_batch(e->p.law, force_args(e, e->items_new, (int32_t)items.size()),
                                  e->occ_acc * e->nsm, e->fblock, e->fipt, e->stream));
     return half_kick(e, slots, 0.5);
@@ -466,38 +486,48 @@ int prepare_chunk(nb_engine* e) {
     return start_systems(e, admitted);
 }
 
-// Launch up to max_steps engine steps (fewer when a system finishes earlier or
-// max_steps_per_call is reached) as graph replays between two events; *k is
-// the step count (0: nothing to run).  No synchronisation.
+// Launch up to max_steps engine steps (at most max_steps_per_call, and no more
+// than the running system with the most steps left needs) as graph replays
+// between two events; *k is the step count (0: nothing to run).  A system that
+// makes its last step inside the chunk is held where it is by the step graph's
+// per-slot gate (steps_slot >= nsteps_slot: no drift, force, kick or count)
+// until the chunk ends and retires it, so chunks need not stop at the first
+// system to finish.  No synchronisation.
 int launch_chunk(nb_engine* e, int64_t max_steps, int64_t* k_out) {
     *k_out = 0;
     if (e->nrank == 0) return NB_OK;
-    int64_t k = std::min<int64_t>(max_steps, e->p.max_steps_per_call);
+    int64_t need = 0, least = INT64_MAX;
     for (int32_t s = 0; s < (int32_t)e->slot_req.size(); ++s) {
         if (e->slot_req[s] < 0) continue;
         const Request& q = e->reqs[e->slot_req[s]];
-        if (q.state == NB_REQ_RUNNING) k = std::min<int64_t>(k, q.nsteps - q.steps_done);
+        if (q.state != NB_REQ_RUNNING) continue;
+        need = std::max<int64_t>(need, q.nsteps - q.steps_done);
+        least = std::min<int64_t>(least, q.nsteps - q.steps_done);
     }
+    const int64_t k = std::min<int64_t>(std::min<int64_t>(max_steps, e->p.max_steps_per_call), need);
     if (k <= 0) return NB_OK;
-    if (!e->graph) {
+    // the gate is needed only when some system finishes inside the chunk
+    const bool gated = least < k;
+    cudaGraphExec_t* exec = gated ? &e->graph_gated : &e->graph;
+    if (!*exec) {
         cudaGraph_t g = nullptr;
         NE_CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        cudaError_t r1 = enqueue_step(e, e->stream);
+        cudaError_t r1 = enqueue_step(e, e->stream, gated);
         cudaError_t r2 = cudaStreamEndCapture(e->stream, &g);
         if (r1 != cudaSuccess || r2 != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
             return efail(e, NB_ERR_CUDA, "engine step capture failed: %s",
                          cudaGetErrorString(r1 != cudaSuccess ? r1 : r2));
         }
-        cudaError_t r3 = cudaGraphInstantiate(&e->graph, g, 0);
+        cudaError_t r3 = cudaGraphInstantiate(exec, g, 0);
         cudaGraphDestroy(g);
         if (r3 != cudaSuccess) {
-            e->graph = nullptr;
+            *exec = nullptr;
             return efail(e, NB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(r3));
         }
     }
     NE_CK(cudaEventRecord(e->ev0, e->stream));
-    for (int64_t i = 0; i < k; ++i) NE_CK(cudaGraphLaunch(e->graph, e->stream));
+    for (int64_t i = 0; i < k; ++i) NE_CK(cudaGraphLaunch(*exec, e->stream));
     NE_CK(cudaEventRecord(e->ev1, e->stream));
     *k_out = k;
     return NB_OK;
@@ -512,11 +542,13 @@ int complete_chunk(nb_engine* e, int64_t k) {
     NE_CK(cudaEventElapsedTime(&ms, e->ev0, e->ev1));
     e->stats.gpu_ms += ms;
     e->stats.engine_steps += k;
-    e->stats.interactions += (double)k * e->pairs_per_step;
     for (int32_t s = 0; s < (int32_t)e->slot_req.size(); ++s) {
         if (e->slot_req[s] < 0) continue;
         Request& q = e->reqs[e->slot_req[s]];
-        if (q.state == NB_REQ_RUNNING) q.steps_done += k;
+        if (q.state != NB_REQ_RUNNING) continue;
+        const int64_t adv = std::min<int64_t>(k, q.nsteps - q.steps_done);  // the gate stops it there
+        q.steps_done += adv;
+        e->stats.interactions += (double)adv * (double)q.n * (double)q.n;
     }
     return retire(e);
 }
@@ -567,6 +599,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     for (int k = 0; k < 11; ++k) o_d[k] = take(dP);
     size_t o_sys = take(sizeof(int32_t) * P), o_perm = take(sizeof(int32_t) * P);
     size_t o_lperm = take(sizeof(int32_t) * P), o_steps = take(sizeof(int64_t) * S);
+    size_t o_nsteps = take(sizeof(int64_t) * S);
     size_t o_sort = take(nb::sort_scratch_bytes(P));
     size_t o_pack = take(sizeof(float4) * kTile * (size_t)e->tile_cap);
     size_t o_orig = take(sizeof(nb::TileOrigin) * (size_t)e->tile_cap);
@@ -592,6 +625,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     e->perm = (int32_t*)(b + o_perm);
     e->lperm = (int32_t*)(b + o_lperm);
     e->steps_slot = (int64_t*)(b + o_steps);
+    e->nsteps_slot = (int64_t*)(b + o_nsteps);
     e->sort_scratch = b + o_sort;
     e->pack = (float4*)(b + o_pack);
     e->origin = (nb::TileOrigin*)(b + o_orig);

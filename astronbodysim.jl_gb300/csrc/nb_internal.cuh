@@ -229,6 +229,11 @@ struct BatchForce {
     const int32_t* sysid;
     const double* dt_slot;
     const double* fac_slot;
+    // Optional per-slot gate (the engine's step): a system whose own step
+    // count has reached its target (steps_slot[s] >= nsteps_slot[s]) is
+    // skipped, so it stays where its last step left it.
+    const int64_t* steps_slot;
+    const int64_t* nsteps_slot;
 };
 
 cudaError_t launch_force_batch(int law, const BatchForce& f, int grid, int block, int ipt,
@@ -245,19 +250,24 @@ cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot,
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
                               const double* bbox, const int32_t* perm, const double* x,
                               const double* y, const double* z, const double* m, float4* pack,
-                              TileOrigin* origin, float4* ext, cudaStream_t s);
+                              TileOrigin* origin, float4* ext, const int32_t* sysid,
+                              const int64_t* steps_slot, const int64_t* nsteps_slot,
+                              cudaStream_t s);
 int batch_small_sort_limit();
 cudaError_t prepare_batch_sort_small();
 cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t max_small_n,
-                                    const int64_t* steps_slot, int32_t every, int32_t force_all,
-                                    const double* x, const double* y, const double* z,
-                                    double* bbox, int32_t* lperm, cudaStream_t s);
+                                    const int64_t* steps_slot, const int64_t* nsteps_slot,
+                                    int32_t every, int32_t force_all, const double* x,
+                                    const double* y, const double* z, double* bbox, int32_t* lperm,
+                                    cudaStream_t s);
 cudaError_t launch_batch_perm_to_local(const BatchSys* bs, int32_t nrank, const int32_t* perm,
                                        int32_t* lperm, cudaStream_t s);
-cudaError_t launch_batch_tick(const BatchSys* bs, int32_t nrank, int64_t* steps_slot, cudaStream_t s);
+cudaError_t launch_batch_tick(const BatchSys* bs, int32_t nrank, int64_t* steps_slot,
+                              const int64_t* nsteps_slot, cudaStream_t s);
 cudaError_t launch_batch_drift(double* x, double* y, double* z, const double* vx, const double* vy,
                                const double* vz, const int32_t* sysid, const double* dt_slot,
-                               const double* fac_slot, int64_t n, cudaStream_t s);
+                               const double* fac_slot, const int64_t* steps_slot,
+                               const int64_t* nsteps_slot, int64_t n, cudaStream_t s);
 cudaError_t launch_batch_kick(double* vx, double* vy, double* vz, const double* ax,
                               const double* ay, const double* az, const int32_t* sysid,
                               const double* dt_slot, const double* fac_slot, int64_t n,

@@ -347,9 +347,13 @@ int nb_engine_destroy(nb_engine *e);
 int nb_batch_submit(nb_engine *e, int64_t n, const double *x, const double *y, const double *z,
                     const double *vx, const double *vy, const double *vz, const double *m,
                     double softening, double dt, int64_t nsteps, int64_t *id);
-/* Admit what fits, then advance every resident system by up to max_steps steps
- * (fewer when a system finishes earlier or max_steps_per_call is reached);
- * finished systems are retired and their results kept for nb_batch_fetch. */
+/* Admit what fits, then run a chunk of up to max_steps engine steps (at most
+ * max_steps_per_call, and no more than the resident system with the most
+ * steps left needs).  Every resident system advances one KDK step per engine
+ * step until it has made its nsteps; a system that finishes inside the chunk
+ * is held on the device where its last step left it (no drift, force or kick)
+ * until the chunk ends.  *steps_done = engine steps of the chunk.  Finished
+ * systems are then retired and their results kept for nb_batch_fetch. */
 int nb_engine_run(nb_engine *e, int64_t max_steps, int64_t *steps_done);
 /* The same as nb_engine_run, but the chunk of steps is only launched: the
  * call returns while the GPU works, so the caller can build and submit new

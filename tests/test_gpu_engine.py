@@ -225,3 +225,35 @@ def test_run_async_matches_blocking_run(nb):
     for k in range(5):
         np.testing.assert_array_equal(out[("async", k)]["pos"], out[("blocking", k)]["pos"])
         np.testing.assert_array_equal(out[("async", k)]["vel"], out[("blocking", k)]["vel"])
+
+
+def test_systems_finishing_inside_a_chunk_are_held(nb):
+    """A chunk runs as long as the resident system with the most steps left
+    needs (up to max_steps_per_call); a system that makes its last step
+    inside it is held on the device (no drift, force, kick or count) until the
+    chunk ends.  Its result is bit-identical to running it alone, including a
+    system of 0 steps (only the two half kicks), and the interaction count
+    covers the steps actually made."""
+    ds = systems(nb, [700, 1500, 300], seed=81)
+    steps = [5, 40, 0]
+    dt = 1e-3
+    alone = []
+    for d, k in zip(ds, steps):
+        e1 = nb.Engine(max_particles=1 << 13, max_systems=4, max_steps_per_call=16)
+        r = e1.submit(d, 0.01, dt, k)
+        e1.run_until_idle()
+        alone.append(e1.fetch(r, d["pos"].shape[0]))
+        e1.close()
+    eng = nb.Engine(max_particles=1 << 13, max_systems=4, max_steps_per_call=16)
+    ids = [eng.submit(d, 0.01, dt, k) for d, k in zip(ds, steps)]
+    assert eng.run() == 16                       # set by the 40-step system, not the 5-step one
+    assert eng.poll(ids[0]) == (nb._lib.NB_REQ_DONE, 5)
+    assert eng.poll(ids[2]) == (nb._lib.NB_REQ_DONE, 0)
+    assert eng.poll(ids[1]) == (nb._lib.NB_REQ_RUNNING, 16)
+    eng.run_until_idle()
+    for d, rid, ref in zip(ds, ids, alone):
+        got = eng.fetch(rid, d["pos"].shape[0])
+        np.testing.assert_array_equal(got["pos"], ref["pos"])
+        np.testing.assert_array_equal(got["vel"], ref["vel"])
+    st = eng.stats()
+    assert st["interactions"] == pytest.approx(sum(d["pos"].shape[0] ** 2 * k for d, k in zip(ds, steps)))
