@@ -484,7 +484,7 @@ def run_gpu(args):
     if args.serve_seconds > 0:
         serve_stats = {}
         # the stated stream (overloaded on one GPU) and a sustainable load
-        # (offered ~0.8 of what one GB300 serves), drained to the last request
+        # (offered ~0.65 of what one GB300 serves), drained to the last request
         for name, rate, seconds, drain in (
                 ("lambda_%g" % args.serve_rate, args.serve_rate, args.serve_seconds, False),
                 ("lambda_%g_drained" % args.serve_sustainable_rate, args.serve_sustainable_rate,
