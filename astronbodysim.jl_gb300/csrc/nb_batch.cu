@@ -18,22 +18,41 @@ constexpr int kBThreads = 256;
 
 // Per-rank description of a running system (device memory).
 //   aoff: first arena particle, soff: first sorted slot, n: particles.
+// Order-preserving unsigned image of a double (for atomicMin over boxes).
+__device__ __forceinline__ unsigned long long ord_key(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double ord_value(unsigned long long k) {
+    return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+
+// Box of each large system: blockIdx.y = large index (box_key[6 * it ..]),
+// blockIdx.x = chunk of kBThreads * 4 particles; minima of (x, y, z, -x, -y,
+// -z) by atomicMin, so the box does not depend on the order of the CTAs.
 __global__ void __launch_bounds__(kBThreads)
-    k_batch_bbox(const BatchSys* __restrict__ bs, const double* __restrict__ x,
-                 const double* __restrict__ y, const double* __restrict__ z,
-                 double* __restrict__ bbox) {
+    k_batch_large_box(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks,
+                      const double* __restrict__ x, const double* __restrict__ y,
+                      const double* __restrict__ z, unsigned long long* __restrict__ box_key) {
     __shared__ double red[6][kBThreads / 32];
-    const BatchSys d = bs[blockIdx.x];
+    const int32_t r = ranks[blockIdx.y];
+    const BatchSys d = bs[r];
+    const int64_t i0 = (int64_t)blockIdx.x * kBThreads * 4;
+    if (i0 >= d.n) return;  // CTA-uniform
     double v[6] = {1e300, 1e300, 1e300, 1e300, 1e300, 1e300};
-    for (int64_t i = threadIdx.x; i < d.n; i += kBThreads) {
-        const int64_t p = d.aoff + i;
-        const double a = x[p], b = y[p], c = z[p];
-        v[0] = fmin(v[0], a);
-        v[1] = fmin(v[1], b);
-        v[2] = fmin(v[2], c);
-        v[3] = fmin(v[3], -a);
-        v[4] = fmin(v[4], -b);
-        v[5] = fmin(v[5], -c);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int64_t i = i0 + u * kBThreads + threadIdx.x;
+        if (i < d.n) {
+            const int64_t p = d.aoff + i;
+            const double a = x[p], b = y[p], c = z[p];
+            v[0] = fmin(v[0], a);
+            v[1] = fmin(v[1], b);
+            v[2] = fmin(v[2], c);
+            v[3] = fmin(v[3], -a);
+            v[4] = fmin(v[4], -b);
+            v[5] = fmin(v[5], -c);
+        }
     }
 #pragma unroll
     for (int k = 0; k < 6; ++k)
@@ -44,9 +63,9 @@ __global__ void __launch_bounds__(kBThreads)
         for (int k = 0; k < 6; ++k) red[k][threadIdx.x >> 5] = v[k];
     __syncthreads();
     if (threadIdx.x < 6) {
-        double r = red[threadIdx.x][0];
-        for (int w = 1; w < kBThreads / 32; ++w) r = fmin(r, red[threadIdx.x][w]);
-        bbox[blockIdx.x * 6 + threadIdx.x] = r;
+        double m = red[threadIdx.x][0];
+        for (int w = 1; w < kBThreads / 32; ++w) m = fmin(m, red[threadIdx.x][w]);
+        atomicMin(&box_key[blockIdx.y * 6 + threadIdx.x], ord_key(m));
     }
 }
 
@@ -61,35 +80,33 @@ __device__ __forceinline__ uint64_t spread3_14(uint64_t v) {
     return v;
 }
 
-// key = rank << 42 | Morton code (14 bits per axis over the system's box);
-// free arena space sorts last.
+// key = large index << 42 | Morton code (14 bits per axis over the system's
+// box), at the system's compact offset; vals = arena index.  Within a system
+// the input is in arena order, so the stable sort breaks ties by it.
 __global__ void __launch_bounds__(kBThreads)
-    k_batch_keys(const int32_t* __restrict__ sysid, const int32_t* __restrict__ rank_of_slot,
-                 const double* __restrict__ bbox, const double* __restrict__ x,
-                 const double* __restrict__ y, const double* __restrict__ z, int64_t n,
-                 uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    k_batch_large_keys(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks,
+                       const unsigned long long* __restrict__ box_key, const double* __restrict__ x,
+                       const double* __restrict__ y, const double* __restrict__ z,
+                       uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    const int32_t lr = blockIdx.y;
+    const int32_t r = ranks[lr];
+    const BatchSys d = bs[r];
     const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
-    if (i >= n) return;
-    const int32_t s = sysid[i];
-    const int32_t r = s >= 0 ? rank_of_slot[s] : -1;
-    uint64_t key = ~0ull;
-    if (r >= 0) {
-        const double* bb = bbox + 6 * (int64_t)r;
-        const double p[3] = {x[i], y[i], z[i]};
-        uint64_t q[3];
+    if (i >= d.n) return;
+    const int64_t p = d.aoff + i;
+    const double pp[3] = {x[p], y[p], z[p]};
+    uint64_t q[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const double lo = bb[k], hi = -bb[3 + k];
-            const double ext = hi - lo;
-            double f = ext > 0.0 ? (p[k] - lo) / ext : 0.0;
-            f = fmin(fmax(f, 0.0), 1.0);
-            q[k] = (uint64_t)(f * 16383.0);
-        }
-        key = ((uint64_t)r << 42) | spread3_14(q[0]) | (spread3_14(q[1]) << 1) |
-              (spread3_14(q[2]) << 2);
+    for (int k = 0; k < 3; ++k) {
+        const double lo = ord_value(box_key[lr * 6 + k]), hi = -ord_value(box_key[lr * 6 + 3 + k]);
+        const double ext = hi - lo;
+        double f = ext > 0.0 ? (pp[k] - lo) / ext : 0.0;
+        f = fmin(fmax(f, 0.0), 1.0);
+        q[k] = (uint64_t)(f * 16383.0);
     }
-    keys[i] = key;
-    vals[i] = (int32_t)i;
+    keys[d.soff + i] = ((uint64_t)lr << 42) | spread3_14(q[0]) | (spread3_14(q[1]) << 1) |
+                       (spread3_14(q[2]) << 2);
+    vals[d.soff + i] = (int32_t)p;
 }
 
 // Systems of at most kSmallSort particles are ordered by one CTA each, in
@@ -186,18 +203,16 @@ __global__ void __launch_bounds__(kSortCta)
     for (int i = tid; i < d.n; i += kSortCta) lperm[d.aoff + i] = (int32_t)(sk[i] & 0x3fffull);
 }
 
-// Global radix-sort result of the systems too large for shared memory, as
-// arena-relative local order: lperm[aoff + k] = perm[soff + k] - aoff.
+// Radix-sort result of the large systems as arena-relative local order:
+// lperm[aoff + k] = perm[soff + k] - aoff (grid: chunks x large index).
 __global__ void __launch_bounds__(kBThreads)
-    k_batch_perm_to_local(const BatchSys* __restrict__ bs, const int32_t* __restrict__ perm,
-                          int32_t* __restrict__ lperm) {
-    const BatchSys d = bs[blockIdx.x];
-    if (d.n <= kSmallSort) return;
-    for (int64_t k = threadIdx.x; k < d.n; k += kBThreads)
-        lperm[d.aoff + k] = (int32_t)(perm[d.soff + k] - d.aoff);
+    k_batch_perm_to_local(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks,
+                          const int32_t* __restrict__ perm, int32_t* __restrict__ lperm) {
+    const BatchSys d = bs[ranks[blockIdx.y]];
+    const int64_t k = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
+    if (k < d.n) lperm[d.aoff + k] = (int32_t)(perm[d.soff + k] - d.aoff);
 }
 
-// Per-system step counter (drives the re-ordering schedule).
 // A system whose count has reached its target (nsteps_slot) stops counting.
 __global__ void k_batch_tick(const BatchSys* __restrict__ bs, int32_t nrank,
                              int64_t* __restrict__ steps_slot,
@@ -228,10 +243,12 @@ cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t m
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_perm_to_local(const BatchSys* bs, int32_t nrank, const int32_t* perm,
-                                       int32_t* lperm, cudaStream_t s) {
-    if (nrank <= 0) return cudaSuccess;
-    k_batch_perm_to_local<<<nrank, kBThreads, 0, s>>>(bs, perm, lperm);
+cudaError_t launch_batch_perm_to_local(const BatchSys* bs, const int32_t* ranks, int32_t nlarge,
+                                       int32_t max_n, const int32_t* perm, int32_t* lperm,
+                                       cudaStream_t s) {
+    if (nlarge <= 0 || max_n <= 0) return cudaSuccess;
+    const dim3 grid((unsigned)((max_n + kBThreads - 1) / kBThreads), (unsigned)nlarge);
+    k_batch_perm_to_local<<<grid, kBThreads, 0, s>>>(bs, ranks, perm, lperm);
     return cudaGetLastError();
 }
 
@@ -710,19 +727,17 @@ cudaError_t launch_fill_i32(int32_t* a, int64_t n, int32_t v, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_bbox(const BatchSys* bs, int32_t nrank, const double* x, const double* y,
-                              const double* z, double* bbox, cudaStream_t s) {
-    if (nrank <= 0) return cudaSuccess;
-    k_batch_bbox<<<nrank, kBThreads, 0, s>>>(bs, x, y, z, bbox);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot, const double* bbox,
-                              const double* x, const double* y, const double* z, int64_t n,
-                              uint64_t* keys, int32_t* vals, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    k_batch_keys<<<(unsigned)((n + kBThreads - 1) / kBThreads), kBThreads, 0, s>>>(
-        sysid, rank_of_slot, bbox, x, y, z, n, keys, vals);
+cudaError_t launch_batch_large_keys(const BatchSys* bs, const int32_t* ranks, int32_t nlarge,
+                                    int32_t max_n, const double* x, const double* y, const double* z,
+                                    unsigned long long* box_key, uint64_t* keys, int32_t* vals,
+                                    cudaStream_t s) {
+    if (nlarge <= 0 || max_n <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(box_key, 0xff, sizeof(unsigned long long) * 6 * (size_t)nlarge, s);
+    if (e != cudaSuccess) return e;
+    const dim3 gbox((unsigned)((max_n + 4 * kBThreads - 1) / (4 * kBThreads)), (unsigned)nlarge);
+    k_batch_large_box<<<gbox, kBThreads, 0, s>>>(bs, ranks, x, y, z, box_key);
+    const dim3 gkey((unsigned)((max_n + kBThreads - 1) / kBThreads), (unsigned)nlarge);
+    k_batch_large_keys<<<gkey, kBThreads, 0, s>>>(bs, ranks, box_key, x, y, z, keys, vals);
     return cudaGetLastError();
 }
 

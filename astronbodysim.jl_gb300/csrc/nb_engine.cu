@@ -110,7 +110,13 @@ struct nb_engine {
     int32_t nitems = 0;
     double pairs_per_step = 0.0;
     int32_t max_small_n = 0;   // largest system ordered in shared memory
-    bool global_sort = false;  // some system is too large for the shared-memory sort
+    // systems too large for the shared-memory sort ("large"): their ranks,
+    // particle count and largest size; they are radix-sorted every step
+    int32_t nlarge = 0;
+    int64_t nl_particles = 0;
+    int32_t max_large_n = 0;
+    int32_t* large_ranks = nullptr;        // device, max_systems
+    unsigned long long* box_key = nullptr;  // device, 6 per large system
     cudaGraphExec_t graph = nullptr;        // step graph without the per-slot gate
     cudaGraphExec_t graph_gated = nullptr;  // with it, for chunks some system finishes inside
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -211,6 +217,8 @@ int rebuild(nb_engine* e) {
     std::vector<double> fstep(e->p.max_systems, 0.0), dts(e->p.max_systems, 0.0);
     std::vector<int64_t> nst(e->p.max_systems, 0);
     int64_t soff = 0, toff = 0, hw = 0;
+    std::vector<int32_t> lranks;
+    int32_t max_large = 0;
     double pairs = 0.0;
     for (int32_t r = 0; r < R; ++r) {
         const Request& q = e->reqs[e->slot_req[slots[r]]];
@@ -225,13 +233,20 @@ int rebuild(nb_engine* e) {
         d.nblocks = (int32_t)((q.n + bt - 1) / bt);
         for (int k = 0; k < 6; ++k) d.soft[k] = q.soft;
         sd[r] = d;
-        bs[r] = nb::BatchSys{q.aoff, soff, (int32_t)q.n, slots[r]};
+        // sorted-slot offset: compact over the large systems (the only ones
+        // the radix sort orders); unused by the others
+        const bool large = q.n > nb::batch_small_sort_limit();
+        bs[r] = nb::BatchSys{q.aoff, large ? soff : 0, (int32_t)q.n, slots[r]};
+        if (large) {
+            lranks.push_back(r);
+            max_large = std::max<int32_t>(max_large, (int32_t)q.n);
+            soff += q.n;
+        }
         ros[slots[r]] = r;
         for (int64_t t = 0; t < nt; ++t) trank.push_back(r);
         fstep[slots[r]] = 1.0;
         dts[slots[r]] = q.dt;
         nst[slots[r]] = q.nsteps;
-        soff += q.n;
         toff += nt;
         hw = std::max(hw, q.aoff + q.n);
         pairs += (double)q.n * (double)q.n;
@@ -262,13 +277,14 @@ int rebuild(nb_engine* e) {
     e->high_water = hw;
     e->pairs_per_step = pairs;
     e->max_small_n = 0;
-    e->global_sort = false;
-    for (int32_t r = 0; r < R; ++r) {
-        if (sd[r].n <= nb::batch_small_sort_limit())
-            e->max_small_n = std::max(e->max_small_n, sd[r].n);
-        else
-            e->global_sort = true;
-    }
+    for (int32_t r = 0; r < R; ++r)
+        if (sd[r].n <= nb::batch_small_sort_limit()) e->max_small_n = std::max(e->max_small_n, sd[r].n);
+    e->nlarge = (int32_t)lranks.size();
+    e->nl_particles = soff;
+    e->max_large_n = max_large;
+    if (!lranks.empty())
+        NE_CK(cudaMemcpy(e->large_ranks, lranks.data(), sizeof(int32_t) * lranks.size(),
+                         cudaMemcpyHostToDevice));
     e->dirty = false;
     drop_graph(e);
     return NB_OK;
@@ -308,16 +324,23 @@ nb::BatchForce force_args(nb_engine* e, const int2* items, int32_t nitems) {
 cudaError_t enqueue_sort_pack(nb_engine* e, cudaStream_t s, bool force_all, bool gate) {
     const int64_t* nsteps = gate ? e->nsteps_slot : nullptr;
     cudaError_t r = cudaSuccess;
-    if (e->global_sort) {
-        r = nb::launch_batch_bbox(e->batchsys, e->nrank, e->x, e->y, e->z, e->bbox, s);
+    if (e->nlarge > 0) {
+        // the large systems' particles only; digits up to the large index bits
+        const int64_t nl = e->nl_particles;
+        int bits = 42, v = e->nlarge - 1;
+        while (v > 0) {
+            ++bits;
+            v >>= 1;
+        }
+        const int passes = ((bits + 7) / 8 + 1) / 2 * 2;  // 8-bit digits, an even count
+        r = nb::launch_batch_large_keys(e->batchsys, e->large_ranks, e->nlarge, e->max_large_n, e->x,
+                                        e->y, e->z, e->box_key, nb::sort_keys_buffer(e->sort_scratch, nl),
+                                        e->perm, s);
         if (r != cudaSuccess) return r;
-        r = nb::launch_batch_keys(e->sysid, e->rank_of_slot, e->bbox, e->x, e->y, e->z,
-                                  e->high_water, nb::sort_keys_buffer(e->sort_scratch, e->high_water),
-                                  e->perm, s);
+        r = nb::launch_sort_keys(e->sort_scratch, nl, e->perm, passes, s);
         if (r != cudaSuccess) return r;
-        r = nb::launch_sort_keys(e->sort_scratch, e->high_water, e->perm, 8, s);
-        if (r != cudaSuccess) return r;
-        r = nb::launch_batch_perm_to_local(e->batchsys, e->nrank, e->perm, e->lperm, s);
+        r = nb::launch_batch_perm_to_local(e->batchsys, e->large_ranks, e->nlarge, e->max_large_n,
+                                           e->perm, e->lperm, s);
         if (r != cudaSuccess) return r;
     }
     r = nb::launch_batch_sort_small(e->batchsys, e->nrank, e->max_small_n, e->steps_slot, nsteps,
@@ -609,6 +632,7 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     size_t o_ros = take(sizeof(int32_t) * S), o_bbox = take(sizeof(double) * 6 * S);
     size_t o_dt = take(sizeof(double) * S), o_fs = take(sizeof(double) * S);
     size_t o_fo = take(sizeof(double) * S);
+    size_t o_lr = take(sizeof(int32_t) * S), o_bk = take(sizeof(unsigned long long) * 6 * S);
     // work items: at most one per i-block of the smallest block (128 targets) per system
     e->item_cap = P / 128 + S;
     size_t o_it = take(sizeof(int2) * (size_t)e->item_cap), o_itn = take(sizeof(int2) * (size_t)e->item_cap);
@@ -638,6 +662,8 @@ int nb_engine_create(const nb_engine_params* p, nb_engine** out) {
     e->dt_slot = (double*)(b + o_dt);
     e->fac_step = (double*)(b + o_fs);
     e->fac_once = (double*)(b + o_fo);
+    e->large_ranks = (int32_t*)(b + o_lr);
+    e->box_key = (unsigned long long*)(b + o_bk);
     e->items = (int2*)(b + o_it);
     e->items_new = (int2*)(b + o_itn);
     e->counter = (int32_t*)(b + o_cnt);

@@ -242,11 +242,17 @@ cudaError_t launch_fill_i32(int32_t* a, int64_t n, int32_t v, cudaStream_t s);
 int batch_ctas_per_sm(int law, bool acc, bool pot, int block, int ipt);
 bool batch_shape_ok(int block, int ipt);
 int batch_block_targets(int block, int ipt);
-cudaError_t launch_batch_bbox(const BatchSys* bs, int32_t nrank, const double* x, const double* y,
-                              const double* z, double* bbox, cudaStream_t s);
-cudaError_t launch_batch_keys(const int32_t* sysid, const int32_t* rank_of_slot, const double* bbox,
-                              const double* x, const double* y, const double* z, int64_t n,
-                              uint64_t* keys, int32_t* vals, cudaStream_t s);
+// Morton order of the systems too large for the shared-memory sort ("large"
+// systems, listed by rank in ranks[0 .. nlarge)): their particles only, at
+// compact offsets BatchSys::soff (0 .. nl), are keyed (large index << 42 |
+// 14-bit-per-axis Morton code over the system's box) and radix-sorted.  The
+// boxes are reduced with atomics on order-preserving integer images of the
+// coordinates into box_key (6 per large system, reset to all ones first).
+// Grids are (chunks of the largest system) x nlarge.
+cudaError_t launch_batch_large_keys(const BatchSys* bs, const int32_t* ranks, int32_t nlarge,
+                                    int32_t max_n, const double* x, const double* y, const double* z,
+                                    unsigned long long* box_key, uint64_t* keys, int32_t* vals,
+                                    cudaStream_t s);
 cudaError_t launch_batch_pack(const int32_t* tile_rank, int32_t ntiles, const SysDesc* sys,
                               const double* bbox, const int32_t* perm, const double* x,
                               const double* y, const double* z, const double* m, float4* pack,
@@ -260,8 +266,9 @@ cudaError_t launch_batch_sort_small(const BatchSys* bs, int32_t nrank, int32_t m
                                     int32_t every, int32_t force_all, const double* x,
                                     const double* y, const double* z, double* bbox, int32_t* lperm,
                                     cudaStream_t s);
-cudaError_t launch_batch_perm_to_local(const BatchSys* bs, int32_t nrank, const int32_t* perm,
-                                       int32_t* lperm, cudaStream_t s);
+cudaError_t launch_batch_perm_to_local(const BatchSys* bs, const int32_t* ranks, int32_t nlarge,
+                                       int32_t max_n, const int32_t* perm, int32_t* lperm,
+                                       cudaStream_t s);
 cudaError_t launch_batch_tick(const BatchSys* bs, int32_t nrank, int64_t* steps_slot,
                               const int64_t* nsteps_slot, cudaStream_t s);
 cudaError_t launch_batch_drift(double* x, double* y, double* z, const double* vx, const double* vy,

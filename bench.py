@@ -581,8 +581,13 @@ def run_ensemble(nb, args, rank=0, local=0):
     args.batch_steps KDK steps; aggregate interactions/s over the engine's
     CUDA-event time."""
     ens = nb.ensemble_systems(args.batch_systems, seed=11 + rank)
+    # optional large systems among the small ones (the tail of whole-i-block
+    # work items: a large system's i-block sweeps all of its j-tiles)
+    for k in range(args.batch_big):
+        ens.append((nb.plummer(args.batch_big_n, seed=500 + k), 1e-3))
     tot = sum(d["pos"].shape[0] for d, _ in ens)
-    eng = nb.Engine(max_particles=tot + 4096, max_systems=args.batch_systems,
+    nsys = len(ens)
+    eng = nb.Engine(max_particles=tot + 4096, max_systems=nsys,
                     max_steps_per_call=args.batch_steps, device=local, law=args.law, tuning="auto")
     for d, eps in ens:
         eng.submit(d, eps, 1e-3, args.batch_steps)
@@ -593,7 +598,8 @@ def run_ensemble(nb, args, rank=0, local=0):
     st = eng.stats()
     eng.close()
     return {"value": st["interactions"] / (st["gpu_ms"] / 1e3) / 1e9, "unit": UNIT,
-            "systems": args.batch_systems, "particles": tot, "steps": args.batch_steps,
+            "systems": nsys, "large_systems": [args.batch_big, args.batch_big_n],
+            "particles": tot, "steps": args.batch_steps,
             "interactions": st["interactions"], "gpu_s": st["gpu_ms"] / 1e3,
             "wall_s_incl_admission_and_retirement": t_batch_wall,
             "force_shape": "%dx%d (block x targets/thread)" % eng.shape,
@@ -792,6 +798,8 @@ def main():
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--skip-batch", action="store_true")
     ap.add_argument("--batch-systems", type=int, default=4096)
+    ap.add_argument("--batch-big", type=int, default=0, help="extra Plummer systems of --batch-big-n particles")
+    ap.add_argument("--batch-big-n", type=int, default=65536)
     ap.add_argument("--batch-steps", type=int, default=1000)
     ap.add_argument("--serve-seconds", type=float, default=20.0)
     ap.add_argument("--serve-rate", type=float, default=200.0)

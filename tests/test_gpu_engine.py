@@ -257,3 +257,34 @@ def test_systems_finishing_inside_a_chunk_are_held(nb):
         np.testing.assert_array_equal(got["vel"], ref["vel"])
     st = eng.stats()
     assert st["interactions"] == pytest.approx(sum(d["pos"].shape[0] ** 2 * k for d, k in zip(ds, steps)))
+
+
+def test_large_systems_alone_and_in_the_mix(nb):
+    """Systems above the shared-memory sort limit (16384) are ordered by a radix
+    sort over their own particles only, at compact offsets.  Two of them among
+    small systems end bit-identical to each running alone, whatever their
+    ranks and arena places."""
+    big = systems(nb, [20000, 17000], seed=91)
+    small = systems(nb, [900, 3000, 500], seed=95)
+    dt, steps = 1e-3, 12
+    alone = []
+    for d in big:
+        e1 = nb.Engine(max_particles=1 << 16, max_systems=4, max_steps_per_call=5)
+        r = e1.submit(d, 0.005, dt, steps)
+        e1.run_until_idle()
+        alone.append(e1.fetch(r, d["pos"].shape[0]))
+        e1.close()
+    eng = nb.Engine(max_particles=1 << 17, max_systems=8, max_steps_per_call=5)
+    s0 = eng.submit(small[0], 0.01, dt, 30)
+    b0 = eng.submit(big[0], 0.005, dt, steps)
+    s1 = eng.submit(small[1], 0.01, dt, 7)
+    eng.run(3)
+    b1 = eng.submit(big[1], 0.005, dt, steps)
+    s2 = eng.submit(small[2], 0.01, dt, 9)
+    eng.run_until_idle()
+    for rid, d, ref in ((b0, big[0], alone[0]), (b1, big[1], alone[1])):
+        got = eng.fetch(rid, d["pos"].shape[0])
+        np.testing.assert_array_equal(got["pos"], ref["pos"])
+        np.testing.assert_array_equal(got["vel"], ref["vel"])
+    for rid in (s0, s1, s2):
+        assert eng.poll(rid)[0] == nb._lib.NB_REQ_DONE
