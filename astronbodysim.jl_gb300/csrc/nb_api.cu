@@ -78,18 +78,20 @@ namespace {
 
 constexpr int kTileJ = 256;
 // Built-in launch rule (the autotuner's choices on GB300, both laws, rounded
-// to three size classes): the direct grid of 128-thread CTAs with each
+// to four size classes): the direct grid of 128-thread CTAs with each
 // i-block's tiles split over several CTAs --
-//   N <  2^16: one target per thread, j-split 4, tiles of 256;
+//   N <  2^15: one target per thread, j-split 4, tiles of 128;
+//   N >= 2^15: one target per thread, j-split 8, tiles of 256;
 //   N >= 2^16: two targets per thread, j-split 8, tiles of 256;
 //   N >= 2^17: the same with tiles of 512 (N = 2^20: 345 ms per force against
-//              367 ms for the first rule).
+//              367 ms with tiles of 256).
 constexpr int kAutoJsplitMax = 8;
+constexpr int64_t kAutoTile256From = 1 << 15;
 constexpr int64_t kAutoIpt2From = 1 << 16;
 constexpr int64_t kAutoTile512From = 1 << 17;
 
-int auto_jsplit(int64_t n) { return n >= kAutoIpt2From ? 8 : 4; }
-int auto_tile(int64_t n) { return n >= kAutoTile512From ? 512 : 256; }
+int auto_jsplit(int64_t n) { return n >= kAutoTile256From ? 8 : 4; }
+int auto_tile(int64_t n) { return n >= kAutoTile512From ? 512 : (n >= kAutoTile256From ? 256 : 128); }
 
 // Reason the last nb_create on this thread failed (there is no handle to hold it).
 thread_local std::string g_create_err;
@@ -277,8 +279,8 @@ cudaError_t enqueue_force(nb_handle* h, const nb::Targets& tg, cudaStream_t s, b
     }
     e = nb::launch_pack(h->x, h->y, h->z, h->m, h->n, h->perm, h->tj, h->pack, h->origin, h->ext, s);
     if (e != cudaSuccess) return e;
-    // Built-in choice (the size classes of kAutoIpt2From / kAutoTile512From
-    // above): the direct grid with each i-block's tiles split over 4 or 8
+    // Built-in choice (the size classes of auto_tile / auto_jsplit above):
+    // the direct grid with each i-block's tiles split over 4 or 8
     // CTAs, whose compensated partials are joined in order.  The split keeps
     // the grid several waves deep at small N and its last wave short at large
     // N.

@@ -43,7 +43,15 @@ __global__ void __launch_bounds__(TJ) k_pack(const double* __restrict__ x,
                                                  float4* __restrict__ pack,
                                                  TileOrigin* __restrict__ origin,
                                                  float4* __restrict__ ext) {
-    __shared__ double red[8][TJ / 32];
+    // Each particle is split once into a double-float pair (12 FP64-pipe
+    // operations, the slow pipe on this GPU).  The tile's box is reduced in
+    // FP32 from the pairs relative to the tile's first particle c, the
+    // common-mass test compares bit patterns, and thread 0 alone forms the
+    // FP64 tile origin c + float offset and shares it.
+    __shared__ float red[6][TJ / 32];
+    __shared__ double cref[4];
+    __shared__ float2 csplit[3];
+    __shared__ TileOrigin tile_o;
     const int64_t i = (int64_t)blockIdx.x * TJ + threadIdx.x;
     const bool valid = i < n;
     double px = 0.0, py = 0.0, pz = 0.0, pm = 0.0;
@@ -54,61 +62,82 @@ __global__ void __launch_bounds__(TJ) k_pack(const double* __restrict__ x,
         pz = z[p];
         pm = m[p];
     }
-    // bounding box (v[0..5]) and the smallest / largest mass (v[6], -v[7])
-    double v[8];
-    v[0] = valid ? px : 1e300;
-    v[1] = valid ? py : 1e300;
-    v[2] = valid ? pz : 1e300;
-    v[3] = valid ? -px : 1e300;
-    v[4] = valid ? -py : 1e300;
-    v[5] = valid ? -pz : 1e300;
-    v[6] = valid ? pm : 1e300;
-    v[7] = valid ? -pm : 1e300;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v[k] = fmin(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
+    const float2 sx = split_df(px), sy = split_df(py), sz = split_df(pz);
+    if (threadIdx.x == 0) {  // every tile holds at least one particle (tiles cover [0, n))
+        cref[0] = px;
+        cref[1] = py;
+        cref[2] = pz;
+        cref[3] = pm;
+        csplit[0] = sx;
+        csplit[1] = sy;
+        csplit[2] = sz;
     }
+    __syncthreads();
+    const double m0 = cref[3];
+    // offsets from c for the box (within a few FP32 ulp of the FP64 offsets;
+    // the box is enlarged below to cover that)
+    const float fx = rel_df(sx, csplit[0].x, csplit[0].y);
+    const float fy = rel_df(sy, csplit[1].x, csplit[1].y);
+    const float fz = rel_df(sz, csplit[2].x, csplit[2].y);
+    const bool same_mass = !valid || __double_as_longlong(pm) == __double_as_longlong(m0);
+    float v[6];
+    v[0] = valid ? fx : 3e38f;
+    v[1] = valid ? fy : 3e38f;
+    v[2] = valid ? fz : 3e38f;
+    v[3] = valid ? -fx : 3e38f;
+    v[4] = valid ? -fy : 3e38f;
+    v[5] = valid ? -fz : 3e38f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = fminf(v[k], __shfl_xor_sync(0xffffffffu, v[k], o));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < 8; ++k) red[k][warp] = v[k];
+        for (int k = 0; k < 6; ++k) red[k][warp] = v[k];
     }
-    __syncthreads();
-    double lo[4], hi[4];
+    const bool uniform = __syncthreads_and(same_mass) && m0 > 0.0;
+    float lo[3], hi[3];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const int ka = k < 3 ? k : 6, kb = k < 3 ? k + 3 : 7;
-        double a = red[ka][0], b = red[kb][0];
+    for (int k = 0; k < 3; ++k) {
+        float a = red[k][0], b = red[k + 3][0];
 #pragma unroll
         for (int w = 1; w < TJ / 32; ++w) {
-            a = fmin(a, red[ka][w]);
-            b = fmin(b, red[kb][w]);
+            a = fminf(a, red[k][w]);
+            b = fminf(b, red[k + 3][w]);
         }
         lo[k] = a;
         hi[k] = -b;
     }
+    const float ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
+    const float amax = fmaxf(fmaxf(fabsf(lo[0]), fabsf(hi[0])),
+                             fmaxf(fmaxf(fabsf(lo[1]), fabsf(hi[1])), fmaxf(fabsf(lo[2]), fabsf(hi[2]))));
+    if (threadIdx.x == 0) {
+        // origin at the box centre; the half diagonal is enlarged to cover the
+        // rounding of the FP32 relative coordinates
+        const float rr = 0.5f * sqrtf(ex * ex + ey * ey + ez * ez);
+        tile_o = make_tile_origin(cref[0] + (double)(0.5f * (lo[0] + hi[0])),
+                                  cref[1] + (double)(0.5f * (lo[1] + hi[1])),
+                                  cref[2] + (double)(0.5f * (lo[2] + hi[2])),
+                                  (double)rr * (1.0 + 1e-5) + 4.0e-7 * (double)amax);
+    }
+    __syncthreads();
+    const TileOrigin to = tile_o;
     // ext.w: the common mass m of the tile's sources when all are equal (the
     // pair loops then apply it once per tile), else 0.  A partial tile stores
     // -m: its far padding adds exactly 0 to the acceleration in that form
     // (r^-3 underflows) but not to the potential, so the potential loops use
     // the per-pair masses there.
     const bool full = ((int64_t)blockIdx.x + 1) * TJ <= n;
-    const float mu = (lo[3] == hi[3] && lo[3] > 0.0) ? (full ? (float)lo[3] : -(float)lo[3]) : 0.0f;
-    // Every tile holds at least one particle (tiles cover [0, n)).
-    const double ox = 0.5 * (lo[0] + hi[0]);
-    const double oy = 0.5 * (lo[1] + hi[1]);
-    const double oz = 0.5 * (lo[2] + hi[2]);
-    const double ex = hi[0] - lo[0], ey = hi[1] - lo[1], ez = hi[2] - lo[2];
-    const TileOrigin to = make_tile_origin(ox, oy, oz, 0.5 * sqrt(ex * ex + ey * ey + ez * ez));
+    const float mu = uniform ? (full ? (float)m0 : -(float)m0) : 0.0f;
     // Sources relative to the origin by the same FP32 steps the force kernels
     // apply to targets (rel_df), so a particle's own source entry and its
     // target coordinates are bit-identical and the self pair has r = 0.
     float qx = 1e18f, qy = 1e18f, qz = 1e18f, qm = 0.0f;
     if (valid) {
-        qx = rel_df(split_df(px), to.hi.x, to.lo.x);
-        qy = rel_df(split_df(py), to.hi.y, to.lo.y);
-        qz = rel_df(split_df(pz), to.hi.z, to.lo.z);
+        qx = rel_df(sx, to.hi.x, to.lo.x);
+        qy = rel_df(sy, to.hi.y, to.lo.y);
+        qz = rel_df(sz, to.hi.z, to.lo.z);
         qm = (float)pm;
     }
     // A full tile of one common mass keeps that mass in ext.w only; its mass
@@ -126,15 +155,12 @@ __global__ void __launch_bounds__(TJ) k_pack(const double* __restrict__ x,
     base[8 * pr + 6 + half] = qm;
     if (threadIdx.x == 0) {
         origin[blockIdx.x] = to;
-        // Half extents of the box for the near test, rounded up and enlarged to
-        // cover the rounding of the FP32 relative coordinates (the test must
-        // never under-estimate them).
-        const double amax = fmax(0.5 * ex, fmax(0.5 * ey, 0.5 * ez));
-        const double slack = 4.0e-7 * amax;
-        ext[blockIdx.x] = make_float4(__double2float_ru(0.5 * ex * (1.0 + 1e-5) + slack),
-                                      __double2float_ru(0.5 * ey * (1.0 + 1e-5) + slack),
-                                      __double2float_ru(0.5 * ez * (1.0 + 1e-5) + slack),
-                                      mu);
+        // Half extents of the box for the near test, enlarged to cover the
+        // rounding of the FP32 relative coordinates (the test must never
+        // under-estimate them).
+        const float slack = 4.0e-7f * amax;
+        ext[blockIdx.x] = make_float4(0.5f * ex * (1.0f + 1e-5f) + slack, 0.5f * ey * (1.0f + 1e-5f) + slack,
+                                      0.5f * ez * (1.0f + 1e-5f) + slack, mu);
     }
 }
 
@@ -358,10 +384,13 @@ __global__ void __launch_bounds__(BLOCK, (ForceOcc<BLOCK, IPT, POT>::value)) k_f
 }
 
 // Adds the j-split partials of every target in part order (deterministic).
+// FP64 adds run on the slow pipe: CTAs of kJoinThreads spread a small target
+// set over many SMs.
+constexpr int kJoinThreads = 64;
 template <int LAW, bool ACC, bool POT>
-__global__ void __launch_bounds__(256) k_force_join(Sources32 src, Targets tg, double G) {
+__global__ void __launch_bounds__(kJoinThreads) k_force_join(Sources32 src, Targets tg, double G) {
     const int64_t ntg = tg.d_count ? (int64_t)(*tg.d_count) : tg.n;
-    const int64_t slot = (int64_t)blockIdx.x * 256 + threadIdx.x;
+    const int64_t slot = (int64_t)blockIdx.x * kJoinThreads + threadIdx.x;
     if (slot >= ntg) return;
     const int32_t p = tg.idx ? tg.idx[slot] : (int32_t)slot;
     double a[4] = {0.0, 0.0, 0.0, 0.0};
@@ -431,7 +460,8 @@ cudaError_t launch_cfg_tile(const Sources32& src, const Targets& tg, double G, u
     if (!launched) return cudaErrorInvalidValue;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || js == 1) return e;
-    k_force_join<LAW, ACC, POT><<<(unsigned)((tg.n + 255) / 256), 256, 0, s>>>(src, tg, G);
+    k_force_join<LAW, ACC, POT><<<(unsigned)((tg.n + kJoinThreads - 1) / kJoinThreads), kJoinThreads, 0, s>>>(
+        src, tg, G);
     return cudaGetLastError();
 }
 

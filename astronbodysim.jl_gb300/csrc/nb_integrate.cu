@@ -9,7 +9,7 @@
 
 namespace nb {
 
-constexpr int kBlock = 256;
+constexpr int kBlock = 128;  // small CTAs spread small systems over more SMs (FP64 work)
 
 static inline unsigned grid_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 

@@ -68,7 +68,9 @@ typedef struct nb_params {
     double time_begin;    /* TimeBegin */
     double time_end;      /* TimeEnd; TimeInterval = (end-begin)/time_base */
     int32_t device;       /* CUDA ordinal */
-    int32_t tile_j;       /* tuning override: sources per j-tile, 128, 256 or 512 (0 = 256) */
+    int32_t tile_j;       /* tuning override: sources per j-tile, 128, 256 or 512 (0: 256 with an
+                             explicit launch shape; with the built-in rule 128 below 2^15
+                             particles, 256 below 2^17, 512 from there) */
     int32_t i_per_thread; /* tuning override (0 = auto) */
     int32_t block;        /* tuning override: threads per CTA of the direct grid (128, 256);
                              -1 = persistent work-list kernel; 0 (with i_per_thread 0) = auto */
