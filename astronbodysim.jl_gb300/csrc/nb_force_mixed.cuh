@@ -384,8 +384,11 @@ __global__ void __launch_bounds__(BLOCK, (ForceOcc<BLOCK, IPT, POT>::value)) k_f
 }
 
 // Adds the j-split partials of every target in part order (deterministic).
-// FP64 adds run on the slow pipe: CTAs of kJoinThreads spread a small target
-// set over many SMs.
+// The compensated (sum, carry) pairs of the parts are added as double-float
+// numbers in FP32 (TwoSum of the sums, carries added), about 48 bits, and
+// converted to FP64 once: the slow FP64 pipe then does two conversions and
+// one add per component instead of two per part.  CTAs of kJoinThreads spread
+// a small target set over many SMs.
 constexpr int kJoinThreads = 64;
 template <int LAW, bool ACC, bool POT>
 __global__ void __launch_bounds__(kJoinThreads) k_force_join(Sources32 src, Targets tg, double G) {
@@ -393,13 +396,18 @@ __global__ void __launch_bounds__(kJoinThreads) k_force_join(Sources32 src, Targ
     const int64_t slot = (int64_t)blockIdx.x * kJoinThreads + threadIdx.x;
     if (slot >= ntg) return;
     const int32_t p = tg.idx ? tg.idx[slot] : (int32_t)slot;
-    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    float s[4] = {0.0f, 0.0f, 0.0f, 0.0f}, c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int part = 0; part < src.jsplit; ++part) {
         const float* q = src.partial + (int64_t)part * 8 * src.pstride + slot;
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-            a[j] += (double)q[(2 * j) * src.pstride] + (double)q[(2 * j + 1) * src.pstride];
+        for (int j = 0; j < 4; ++j) {
+            two_sum_acc(s[j], c[j], q[(2 * j) * src.pstride]);
+            c[j] += q[(2 * j + 1) * src.pstride];
+        }
     }
+    double a[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) a[j] = (double)s[j] + (double)c[j];
     if (ACC) {
         tg.ax[p] = a[0] * G;
         tg.ay[p] = a[1] * G;
