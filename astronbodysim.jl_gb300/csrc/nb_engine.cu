@@ -108,7 +108,6 @@ struct nb_engine {
     int32_t nrank = 0;
     int32_t ntiles_total = 0;
     int32_t nitems = 0;
-    double pairs_per_step = 0.0;
     int32_t max_small_n = 0;   // largest system ordered in shared memory
     // systems too large for the shared-memory sort ("large"): their ranks,
     // particle count and largest size; they are radix-sorted every step
@@ -219,7 +218,6 @@ int rebuild(nb_engine* e) {
     int64_t soff = 0, toff = 0, hw = 0;
     std::vector<int32_t> lranks;
     int32_t max_large = 0;
-    double pairs = 0.0;
     for (int32_t r = 0; r < R; ++r) {
         const Request& q = e->reqs[e->slot_req[slots[r]]];
         const int64_t nt = ntiles_of(q.n);
@@ -249,7 +247,6 @@ int rebuild(nb_engine* e) {
         nst[slots[r]] = q.nsteps;
         toff += nt;
         hw = std::max(hw, q.aoff + q.n);
-        pairs += (double)q.n * (double)q.n;
     }
     // Work items: (rank, i-block), systems with the most j-tiles first.
     std::vector<int32_t> order(R);
@@ -275,7 +272,6 @@ int rebuild(nb_engine* e) {
     e->ntiles_total = (int32_t)toff;
     e->nitems = (int32_t)items.size();
     e->high_water = hw;
-    e->pairs_per_step = pairs;
     e->max_small_n = 0;
     for (int32_t r = 0; r < R; ++r)
         if (sd[r].n <= nb::batch_small_sort_limit()) e->max_small_n = std::max(e->max_small_n, sd[r].n);
