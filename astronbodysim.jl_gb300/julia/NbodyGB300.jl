@@ -137,7 +137,7 @@ function field_params(sim, bgfield)
     error("bgfield must be a PointMassField or a PseudoNewtonianField")
 end
 
-function params(sim; precision = Int32(1), law = Int32(0), bgfield = nothing)
+function params(sim; precision = Int32(1), law = Int32(0), bgfield = nothing, resort_every = 0)
     tc = sim.config.time
     step = tc.step
     soft = ntuple(k -> strip(lenunit(sim), sim.config.grav.ForceSofteningTable[k]), 6)
@@ -159,11 +159,11 @@ function params(sim; precision = Int32(1), law = Int32(0), bgfield = nothing)
              bg_kind, mond, bg_gm, bg_center, bg_rg,
              mond == 0 ? 0.0 : strip(accunit(sim), sim.config.constants.ACC0),
              Float64(sim.config.grav.MOND_nuIndex),
-             Int32(0), Int32(0))       # stages (built-in), resort_every (16)
+             Int32(0), Int32(resort_every))  # stages (built-in), resort_every (0 = 16)
 end
 
 """
-    route(sim; precision = :mixed, law = :spline, bgfield = nothing)
+    route(sim; precision = :mixed, law = :spline, bgfield = nothing, resort_every = 0)
 
 Uploads the particles of a `(DirectSum, GPU)` simulation built by the
 reference's constructor (replacing its `cu(StructArray(d))` placement,
@@ -171,9 +171,11 @@ src/base/Config.jl:1072-1088) and returns the routed simulation.  The
 snapshot schedule (`TimeBetweenSnapshots`, src/base/Config.jl:436-439,
 749-750) goes to the device so that `step` splits its drifts at output times.
 `law = :plummer` selects the r^2 + h^2 softening instead of the reference's
-Gadget-2 spline; `precision = :fp64` the plain FP64 form.
+Gadget-2 spline; `precision = :fp64` the plain FP64 form.  `resort_every`
+sets the steps between Morton re-orders of the sources in `step` (0 = 16,
+1 = every step; the forces differ only by FP32 round-off).
 """
-function route(sim::Simulation; precision = :mixed, law = :spline, bgfield = nothing)
+function route(sim::Simulation; precision = :mixed, law = :spline, bgfield = nothing, resort_every = 0)
     sim.config.solver.grav isa DirectSum || error("NbodyGB300 routes DirectSum simulations only")
     sim.config.device.type isa GPU || error("NbodyGB300 routes GPU simulations only")
     if !isempty(sim.bgforce) && bgfield === nothing
@@ -181,7 +183,7 @@ function route(sim::Simulation; precision = :mixed, law = :spline, bgfield = not
               "as bgfield = PointMassField(GM, center) or PseudoNewtonianField(GM, rg, center)")
     end
     p = Ref(params(sim; precision = Int32(precision === :fp64 ? 0 : 1),
-                   law = Int32(law === :plummer ? 1 : 0), bgfield))
+                   law = Int32(law === :plummer ? 1 : 0), bgfield, resort_every))
     out = Ref{Ptr{Cvoid}}(C_NULL)
     rc = ccall((:nb_create, libnb), Cint, (Ref{NbParams}, Ref{Ptr{Cvoid}}), p, out)
     check(C_NULL, rc)  # with a null handle nb_last_error gives the reason nb_create failed
