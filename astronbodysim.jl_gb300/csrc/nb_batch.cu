@@ -4,20 +4,28 @@
 // contiguous range of arena particles, and every particle carries its slot
 // (sysid, -1 for free space).  The running systems are ranked 0..R-1; a step
 // of the engine is
-//   drift -> per-system bounding boxes -> Morton keys with the rank in the top
-//   bits -> radix sort (systems stay contiguous, each in its own Z-order) ->
-//   per-system packed FP32 tiles -> force over whole i-blocks -> kick.
-// The force kernel never splits an i-block and a system's sort key depends only
+//   drift -> Morton order per system (small systems in shared memory at
+//   admission and every 64 of their own steps; large ones by a radix sort of
+//   their own particles every step) -> per-system packed FP32 tiles -> force
+//   over whole i-blocks with the kick in its epilogue -> step counter.
+// The force kernel never splits an i-block and a system's order depends only
 // on its own particles, so a system's trajectory is bit-identical whether it
 // runs alone or among others.
+#include <algorithm>
+
 #include "nb_pairs.cuh"
 
 namespace nb {
 
 constexpr int kBThreads = 256;
 
-// Per-rank description of a running system (device memory).
-//   aoff: first arena particle, soff: first sorted slot, n: particles.
+// gridDim.y limit: launches over the large systems go in slabs of this many.
+constexpr int32_t kMaxGridY = 65535;
+
+// BatchSys (per rank, device memory): aoff = first arena particle, soff =
+// first slot of the large systems' sort (compact over the large systems),
+// n = particles, slot = system slot.
+
 // Order-preserving unsigned image of a double (for atomicMin over boxes).
 __device__ __forceinline__ unsigned long long ord_key(double v) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
@@ -31,11 +39,12 @@ __device__ __forceinline__ double ord_value(unsigned long long k) {
 // blockIdx.x = chunk of kBThreads * 4 particles; minima of (x, y, z, -x, -y,
 // -z) by atomicMin, so the box does not depend on the order of the CTAs.
 __global__ void __launch_bounds__(kBThreads)
-    k_batch_large_box(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks,
+    k_batch_large_box(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks, int32_t y0,
                       const double* __restrict__ x, const double* __restrict__ y,
                       const double* __restrict__ z, unsigned long long* __restrict__ box_key) {
     __shared__ double red[6][kBThreads / 32];
-    const int32_t r = ranks[blockIdx.y];
+    const int32_t lr = y0 + (int32_t)blockIdx.y;
+    const int32_t r = ranks[lr];
     const BatchSys d = bs[r];
     const int64_t i0 = (int64_t)blockIdx.x * kBThreads * 4;
     if (i0 >= d.n) return;  // CTA-uniform
@@ -65,7 +74,7 @@ __global__ void __launch_bounds__(kBThreads)
     if (threadIdx.x < 6) {
         double m = red[threadIdx.x][0];
         for (int w = 1; w < kBThreads / 32; ++w) m = fmin(m, red[threadIdx.x][w]);
-        atomicMin(&box_key[blockIdx.y * 6 + threadIdx.x], ord_key(m));
+        atomicMin(&box_key[(int64_t)lr * 6 + threadIdx.x], ord_key(m));
     }
 }
 
@@ -84,11 +93,11 @@ __device__ __forceinline__ uint64_t spread3_14(uint64_t v) {
 // box), at the system's compact offset; vals = arena index.  Within a system
 // the input is in arena order, so the stable sort breaks ties by it.
 __global__ void __launch_bounds__(kBThreads)
-    k_batch_large_keys(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks,
+    k_batch_large_keys(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks, int32_t y0,
                        const unsigned long long* __restrict__ box_key, const double* __restrict__ x,
                        const double* __restrict__ y, const double* __restrict__ z,
                        uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
-    const int32_t lr = blockIdx.y;
+    const int32_t lr = y0 + (int32_t)blockIdx.y;
     const int32_t r = ranks[lr];
     const BatchSys d = bs[r];
     const int64_t i = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
@@ -98,7 +107,8 @@ __global__ void __launch_bounds__(kBThreads)
     uint64_t q[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        const double lo = ord_value(box_key[lr * 6 + k]), hi = -ord_value(box_key[lr * 6 + 3 + k]);
+        const double lo = ord_value(box_key[(int64_t)lr * 6 + k]),
+                     hi = -ord_value(box_key[(int64_t)lr * 6 + 3 + k]);
         const double ext = hi - lo;
         double f = ext > 0.0 ? (pp[k] - lo) / ext : 0.0;
         f = fmin(fmax(f, 0.0), 1.0);
@@ -111,8 +121,9 @@ __global__ void __launch_bounds__(kBThreads)
 
 // Systems of at most kSmallSort particles are ordered by one CTA each, in
 // shared memory: FP64 bounding box, 14-bit-per-axis Morton code, bitonic sort
-// of (code << 14 | local index), written to perm[soff .. soff + n).  Keys are
-// unique, so the order depends only on the system's own positions.
+// of (code << 14 | local index), written to lperm[aoff .. aoff + n) as local
+// indices.  Keys are unique, so the order depends only on the system's own
+// positions.
 constexpr int kSmallSort = 16384;
 constexpr int kSortCta = 1024;
 
@@ -206,9 +217,9 @@ __global__ void __launch_bounds__(kSortCta)
 // Radix-sort result of the large systems as arena-relative local order:
 // lperm[aoff + k] = perm[soff + k] - aoff (grid: chunks x large index).
 __global__ void __launch_bounds__(kBThreads)
-    k_batch_perm_to_local(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks,
+    k_batch_perm_to_local(const BatchSys* __restrict__ bs, const int32_t* __restrict__ ranks, int32_t y0,
                           const int32_t* __restrict__ perm, int32_t* __restrict__ lperm) {
-    const BatchSys d = bs[ranks[blockIdx.y]];
+    const BatchSys d = bs[ranks[y0 + (int32_t)blockIdx.y]];
     const int64_t k = (int64_t)blockIdx.x * kBThreads + threadIdx.x;
     if (k < d.n) lperm[d.aoff + k] = (int32_t)(perm[d.soff + k] - d.aoff);
 }
@@ -247,8 +258,11 @@ cudaError_t launch_batch_perm_to_local(const BatchSys* bs, const int32_t* ranks,
                                        int32_t max_n, const int32_t* perm, int32_t* lperm,
                                        cudaStream_t s) {
     if (nlarge <= 0 || max_n <= 0) return cudaSuccess;
-    const dim3 grid((unsigned)((max_n + kBThreads - 1) / kBThreads), (unsigned)nlarge);
-    k_batch_perm_to_local<<<grid, kBThreads, 0, s>>>(bs, ranks, perm, lperm);
+    for (int32_t y0 = 0; y0 < nlarge; y0 += kMaxGridY) {
+        const dim3 grid((unsigned)((max_n + kBThreads - 1) / kBThreads),
+                        (unsigned)std::min<int32_t>(kMaxGridY, nlarge - y0));
+        k_batch_perm_to_local<<<grid, kBThreads, 0, s>>>(bs, ranks, y0, perm, lperm);
+    }
     return cudaGetLastError();
 }
 
@@ -734,10 +748,16 @@ cudaError_t launch_batch_large_keys(const BatchSys* bs, const int32_t* ranks, in
     if (nlarge <= 0 || max_n <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(box_key, 0xff, sizeof(unsigned long long) * 6 * (size_t)nlarge, s);
     if (e != cudaSuccess) return e;
-    const dim3 gbox((unsigned)((max_n + 4 * kBThreads - 1) / (4 * kBThreads)), (unsigned)nlarge);
-    k_batch_large_box<<<gbox, kBThreads, 0, s>>>(bs, ranks, x, y, z, box_key);
-    const dim3 gkey((unsigned)((max_n + kBThreads - 1) / kBThreads), (unsigned)nlarge);
-    k_batch_large_keys<<<gkey, kBThreads, 0, s>>>(bs, ranks, box_key, x, y, z, keys, vals);
+    for (int32_t y0 = 0; y0 < nlarge; y0 += kMaxGridY) {
+        const unsigned ny = (unsigned)std::min<int32_t>(kMaxGridY, nlarge - y0);
+        const dim3 gbox((unsigned)((max_n + 4 * kBThreads - 1) / (4 * kBThreads)), ny);
+        k_batch_large_box<<<gbox, kBThreads, 0, s>>>(bs, ranks, y0, x, y, z, box_key);
+    }
+    for (int32_t y0 = 0; y0 < nlarge; y0 += kMaxGridY) {
+        const unsigned ny = (unsigned)std::min<int32_t>(kMaxGridY, nlarge - y0);
+        const dim3 gkey((unsigned)((max_n + kBThreads - 1) / kBThreads), ny);
+        k_batch_large_keys<<<gkey, kBThreads, 0, s>>>(bs, ranks, y0, box_key, x, y, z, keys, vals);
+    }
     return cudaGetLastError();
 }
 
